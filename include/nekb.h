@@ -1,0 +1,248 @@
+/*
+ * nekb -- GB300-native (sm_103a) spectral-element hot path of nekBench.
+ *
+ * Plain C ABI: device pointers and sizes, no C++ or framework types.  Every
+ * entry point returns NEKB_OK (0) or a negative NEKB_ERR_* status; the text of
+ * the last error on the calling thread is available from nekb_last_error().
+ * Nothing here calls exit() or aborts.  Streams are passed as void* holding a
+ * cudaStream_t (NULL = the legacy default stream).
+ *
+ * Memory layouts follow the reference exactly (paths relative to the nekBench
+ * source tree):
+ *   ggeo    [e*7*Np + slot*Np + n], slots GWJ,G00,G01,G02,G11,G12,G22
+ *           (core/params.h:55-62, core/meshSetup.cpp:342-360)
+ *   q, Aq   [fld*offset + e*Np + i + j*Nq + k*Nq*Nq]      (axhelm.okl:58-61)
+ *   lambda  [id] = lambda0, [id+offset] = lambda1          (axhelm.okl:87-88)
+ *   D       [i*Nq + m] = d l_m / dr at node i              (axhelm.okl:55)
+ * Indices are 64-bit; gather ids are 32-bit like the reference's dlong.
+ */
+#ifndef NEKB_H
+#define NEKB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+#define NEKB_OK                 0
+#define NEKB_ERR_INVALID      (-1)  /* bad argument, size or handle                */
+#define NEKB_ERR_CUDA         (-2)  /* a CUDA call failed                           */
+#define NEKB_ERR_ALLOC        (-3)  /* device or host allocation failed             */
+#define NEKB_ERR_UNSUPPORTED  (-4)  /* order / variant / precision not built        */
+#define NEKB_ERR_BREAKDOWN    (-5)  /* Krylov breakdown (pAp <= 0 or non-finite)    */
+#define NEKB_ERR_NOT_CONVERGED (-6) /* iteration limit reached before tolerance     */
+
+/* axhelm variant bits: the name axhelm[Partial][_bk][_n3]_v0 of the reference
+ * kernels (nekBone/setup.cpp:313-320, axhelm/main.cpp:105-109) maps to
+ * PARTIAL | BK | N3. */
+#define NEKB_AX_BK       1
+#define NEKB_AX_N3       2
+#define NEKB_AX_PARTIAL  4
+
+/* precision of an axhelm application */
+#define NEKB_FP64            0  /* ggeo/lambda/q/Aq double                                   */
+#define NEKB_FP32            1  /* ggeo/lambda/q/Aq float                                    */
+#define NEKB_BF16            2  /* ggeo and lambda bf16 storage, q/Aq float, FP32 arithmetic */
+#define NEKB_FP32_TRILINEAR  3  /* geometry from 24 trilinear coefficients per element
+                                   (float [E][24]) instead of ggeo; q/Aq/lambda float       */
+
+/* gather-scatter data types and ops (3rdParty/ogs/ogs.hpp:128-140) */
+#define NEKB_DOUBLE 0
+#define NEKB_FLOAT  1
+#define NEKB_OP_ADD 0
+
+const char* nekb_last_error(void);
+int nekb_version(void);
+int nekb_device_sync(void);
+/* cudaMemcpy with the direction inferred from the pointers (helper for callers
+ * that hold raw device pointers returned by this library) */
+int nekb_copy(void* dst, const void* src, int64_t bytes);
+
+/* ------------------------------------------------------------------ axhelm
+ * Replaces the OCCA kernels axhelm_v0, axhelm_bk_v0, axhelm_n3_v0,
+ * axhelm_bk_n3_v0 and their Partial forms (axhelm/kernel/VOLTA/axhelm.okl:28,
+ * 158, 292, 484, 671, 865, 1063, 1188) as launched by
+ *   kernel(Nelements, offset, o_ggeo, o_D, o_lambda, o_q, o_Aq)
+ * (nekBone/solve.cpp:218, axhelm/main.cpp:132) and, with NEKB_AX_PARTIAL,
+ *   kernel(Nelements, offset, o_elementList, o_ggeo, o_D, o_lambda, o_q, o_Aq)
+ * (nekBone/solve.cpp:192-200).  Nq = N+1 in [2, 12].  lambda may be NULL in BK
+ * mode.  D is double for NEKB_FP64 and float otherwise.  All pointers are
+ * device pointers. */
+int nekb_axhelm(int Nq, int flags, int precision, int64_t Nelements, int64_t offset,
+                const int32_t* elementList, const void* ggeo, const void* D, const void* lambda,
+                const void* q, void* Aq, void* stream);
+
+/* flags from a reference kernel name such as "axhelmPartial_bk_n3_v0"
+ * (kernel naming of nekBone/setup.cpp:313-320, axhelm/main.cpp:105-109). */
+int nekb_axhelm_flags_from_name(const char* name, int* flags);
+
+/* Jacobi diagonal of the element Helmholtz operator before assembly; nodes
+ * with mapB==1 get 1.  Replaces updateJacobi (nekBone/kernel/updateJacobi.okl:27).
+ * mapB may be NULL (no masked nodes). */
+int nekb_update_jacobi(int Nq, int64_t Nelements, int64_t offset, const int32_t* mapB,
+                       const double* ggeo, const double* D, const double* lambda, double* diag,
+                       void* stream);
+
+/* ------------------------------------------------------------------ geometry
+ * Second-order geometric factors from the element vertices (8 per element,
+ * vertex order of core/meshSetup.cpp:2363-2410) for a trilinear map, at the
+ * GLL nodes r1d with weights w1d; replaces meshGeometricFactorsHex3D
+ * (core/meshSetup.cpp:215-360) for trilinear elements.  EX/EY/EZ, ggeo device
+ * pointers (double); r1d, w1d host arrays of Nq. */
+int nekb_geometric_factors(int Nq, int64_t Nelements, const double* EX, const double* EY,
+                           const double* EZ, const double* r1d, const double* w1d, double* ggeo,
+                           void* stream);
+/* 24 trilinear coefficients per element ([e][c*8+a], float) used by the
+ * NEKB_FP32_TRILINEAR operator. */
+int nekb_trilinear_coeffs(int64_t Nelements, const double* EX, const double* EY, const double* EZ,
+                          float* coef, void* stream);
+
+/* 1D GLL / Gauss nodes and weights and the derivative matrix (host arrays);
+ * restate meshJacobiGL, meshJacobiGQ and meshDmatrix1D (core/meshBasis.cpp:140,
+ * 46, 775). */
+int nekb_gll(int N, double* r, double* w);
+int nekb_gauss(int N, double* r, double* w);
+int nekb_dmatrix(int Nq, const double* r, double* D);
+
+/* seeded uniform numbers in [lo,hi) (device), bit-identical to the CPU
+ * generator used by the tests: value i = lo + (hi-lo)*u(seed, stream, i). */
+int nekb_fill_uniform(double* v, int64_t n, uint64_t seed, uint64_t stream, double lo, double hi,
+                      void* stream_);
+
+/* ------------------------------------------------------------------ gather-scatter
+ * Replaces ogsSetup(N, ids, comm, verbose, device) (3rdParty/ogs/ogs.hpp:178,
+ * src/ogsSetup.cpp:68-355) on one rank: ids==0 nodes are excluded, groups are
+ * numbered by first local appearance, members in ascending local index;
+ * invDegree = 1/multiplicity.  ids is a HOST array of N global ids. */
+typedef struct nekb_ogs nekb_ogs;
+nekb_ogs* nekb_ogs_setup(int64_t N, const int64_t* ids, int verbose, int* status);
+void nekb_ogs_free(nekb_ogs* ogs);
+/* ogsGatherScatterMany(o_v, k, stride, type, op, ogs) (ogs.hpp:200) and
+ * oogs::start/finish (ogs.hpp:259-260): sum over each group, written back to
+ * every member, k fields at the given stride, fixed summation order. */
+int nekb_ogs_gs_many(nekb_ogs* ogs, void* v, int k, int64_t stride, int dtype, int op,
+                     void* stream);
+/* sizes: [0]=N, [1]=Nlocal (ids!=0), [2]=NlocalGather, [3]=groups with >1 member */
+int nekb_ogs_sizes(const nekb_ogs* ogs, int64_t* sizes4);
+/* host copies of the CSR (offsets: NlocalGather+1, ids: Nlocal) for checking */
+int nekb_ogs_copy_csr(const nekb_ogs* ogs, int32_t* offsets, int32_t* ids);
+/* device pointer to invDegree (N doubles), owned by the handle (ogs->o_invDegree) */
+const double* nekb_ogs_inv_degree(const nekb_ogs* ogs);
+
+/* mask kernel (nekBone/kernel/utils.okl:127): q[maskIds[n]] = 0 */
+int nekb_mask(int64_t Nmasked, const int32_t* maskIds, void* q, int dtype, void* stream);
+
+/* ------------------------------------------------------------------ benchmark problem
+ * Box mesh of nx*ny*nz hexahedra of order N on the unit cube, interior vertices
+ * perturbed by U[-perturb*h, perturb*h] (seeded), homogeneous Dirichlet on the
+ * boundary (dirichlet=1) or periodic (periodic=1).  Builds on the device the
+ * geometric factors, gather-scatter handle, mask list and solver workspace:
+ * the state the reference keeps in mesh_t and BP_t (nekBone/BP.hpp:47-153,
+ * nekBone/setup.cpp:36-367). */
+typedef struct nekb_bp nekb_bp;
+typedef struct {
+  int N;
+  int nx, ny, nz;
+  int Nfields;        /* 1 or 3                                            */
+  int periodic;       /* 1: periodic box (no boundary)                      */
+  int dirichlet;      /* 1: boundary nodes masked (ids 0)                   */
+  double perturb;     /* vertex perturbation fraction of h (0.1 typical)    */
+  uint64_t seed;
+} nekb_bp_config;
+
+nekb_bp* nekb_bp_setup(const nekb_bp_config* cfg, void* stream, int* status);
+void nekb_bp_free(nekb_bp* bp);
+/* sizes: [0]=Nq [1]=Nelements [2]=Np [3]=offset (Nlocal) [4]=Nmasked [5]=Nfields */
+int nekb_bp_sizes(const nekb_bp* bp, int64_t* sizes6);
+/* device pointers owned by the problem: name in {"ggeo","D","Df","invDegree",
+ * "maskIds","EX","EY","EZ","x","y","z","trilinear"} */
+void* nekb_bp_device_ptr(nekb_bp* bp, const char* name);
+nekb_ogs* nekb_bp_ogs(nekb_bp* bp);
+
+/* full operator used by the solvers: Aq = mask(gs(axhelm(q))) */
+int nekb_bp_apply(nekb_bp* bp, int bk, int precision, const void* lambda, const void* q, void* Aq);
+
+/* ------------------------------------------------------------------ PCG
+ * BPPCG(BP, o_lambda, o_r, o_x, tol, MAXIT, opElapsed) (nekBone/solve.cpp:44-113,
+ * nekBone/BP.hpp:172-178): r (in: rhs, out: residual) and x (in: guess, out:
+ * solution) are device FP64 arrays of Nfields*offset; lambda device FP64
+ * 2*offset (ignored when bk).  Stops when the invDegree-weighted |r|^2 <=
+ * max(tol^2 |r0|^2, tol^2) (solve.cpp:85,90) or after maxit iterations. */
+#define NEKB_PRECOND_COPY    0
+#define NEKB_PRECOND_JACOBI  1
+#define NEKB_PRECOND_LEARNED 2
+
+#define NEKB_SOLVER_FP64     0   /* plain FP64 PCG (the reference algorithm)          */
+#define NEKB_SOLVER_MIXED    1   /* FP32/BF16 inner PCG inside FP64 iterative refinement */
+
+typedef struct {
+  int solver;           /* NEKB_SOLVER_*                                        */
+  int precond;          /* NEKB_PRECOND_*                                       */
+  int flexible;         /* 1: flexible beta (KRYLOV SOLVER FLEXIBLE)            */
+  int fixed_iterations; /* 1: run exactly maxit iterations                      */
+  int bk;               /* 1: Poisson operator (lambda0=1, lambda1=0)           */
+  int inner_precision;  /* NEKB_FP32, NEKB_BF16 or NEKB_FP32_TRILINEAR (mixed)  */
+  double inner_tol;     /* relative tolerance of each inner solve (mixed)       */
+  int max_outer;        /* refinement steps (mixed)                             */
+  int check_every;      /* iterations between host convergence checks           */
+  int use_graph;        /* 1: replay each chunk of iterations as a CUDA graph   */
+  const void* net;      /* nekb_net* for NEKB_PRECOND_LEARNED                   */
+} nekb_pcg_opts;
+
+typedef struct {
+  int iterations;        /* BPPCG's return value (total inner for mixed)         */
+  int outer_iterations;  /* refinement steps (mixed)                             */
+  int status;            /* NEKB_OK, NEKB_ERR_BREAKDOWN, NEKB_ERR_NOT_CONVERGED  */
+  double rdotr0;         /* weighted |r0|^2                                      */
+  double rdotr;          /* weighted |r|^2 of the last check                     */
+  double true_rel_res;   /* |b - A x|_w / |b|_w in FP64 after the solve          */
+  double elapsed_s;      /* device time of the solve                             */
+} nekb_pcg_stats;
+
+void nekb_pcg_default_opts(nekb_pcg_opts* opts);
+int nekb_bp_pcg(nekb_bp* bp, const double* lambda, double* r, double* x, double tol, int maxit,
+                const nekb_pcg_opts* opts, nekb_pcg_stats* stats);
+
+/* ------------------------------------------------------------------ learned preconditioner
+ * Per-element 3D convolution network: layers of 3x3x3 convolutions on the Nq^3
+ * nodes of each element (zero padding at the element boundary), channels
+ * 1 -> C -> ... -> C -> 1, tanh-form GELU between layers, BF16 weights with
+ * FP32 accumulation.  Used as z = Jacobi(r) + gs(invDegree * net(r_e/|r_e|)*|r_e|)
+ * inside flexible PCG.  No counterpart in the reference (spec extension). */
+typedef struct nekb_net nekb_net;
+nekb_net* nekb_net_create(int Nq, int channels, int layers, uint64_t seed, int* status);
+void nekb_net_free(nekb_net* net);
+int nekb_net_num_params(const nekb_net* net);
+/* FP32 master weights (host arrays of nekb_net_num_params floats) */
+int nekb_net_get_weights(const nekb_net* net, float* w);
+int nekb_net_set_weights(nekb_net* net, const float* w);
+/* forward on E element blocks: in/out device float [E][Nq^3] */
+int nekb_net_forward(nekb_net* net, int64_t E, const float* in, float* out, void* stream);
+/* one training step on a batch: loss = mean_e |net(in_e) - target_e|^2 / Np;
+ * computes gradients with the network's own backward kernels and applies Adam.
+ * loss (host) may be NULL. */
+int nekb_net_train_step(nekb_net* net, int64_t E, const float* in, const float* target, float lr,
+                        float* loss, void* stream);
+/* gradient of the loss w.r.t. the FP32 master weights (host float array), no update */
+int nekb_net_gradient(nekb_net* net, int64_t E, const float* in, const float* target, float* grad,
+                      float* loss, void* stream);
+/* training pairs from solver snapshots: per element e, s_e = RMS(r_e),
+ * in_e = r_e / s_e and target_e = (err_e - invDiag*r_e) / s_e (device float
+ * arrays of E*Np; invDiag of Efield*Np may be NULL) */
+int nekb_net_prepare_pairs(int Np, int64_t E, int64_t Efield, const float* r, const float* err,
+                           const float* invDiag, float* in, float* target, void* stream);
+/* versioned checkpoint (header, sizes, step, weights, Adam moments, CRC-32) */
+int nekb_net_save(const nekb_net* net, const char* path);
+nekb_net* nekb_net_load(const char* path, int* status);
+
+/* ------------------------------------------------------------------ microbenchmarks */
+/* FP64 / FP32 FMA throughput and HBM copy bandwidth of the current device */
+int nekb_peak_fma(int fp64, double* tflops);
+int nekb_peak_copy(double* gbs);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,70 @@
+// Benchmark-problem state (mesh, geometry, gather-scatter, solver workspace):
+// the data the reference keeps in mesh_t and BP_t (nekBone/BP.hpp:47-153).
+#pragma once
+
+#include "internal.h"
+
+#include <map>
+#include <tuple>
+
+namespace nekb {
+
+// operator Aq = mask(gs(axhelm(q))) in one precision
+struct OpView {
+  int Nq = 0;
+  int flags = 0;       // NEKB_AX_BK / NEKB_AX_N3
+  int precision = 0;   // NEKB_FP64, NEKB_FP32, NEKB_BF16, NEKB_FP32_TRILINEAR
+  int Nfields = 1;
+  int64_t E = 0;
+  int64_t offset = 0;  // field stride (= E*Np)
+  const void* ggeo = nullptr;
+  const void* D = nullptr;
+  const void* lambda = nullptr;
+  const nekb_ogs* ogs = nullptr;
+  const int32_t* mask = nullptr;
+  int64_t Nmasked = 0;
+  float r1d[kMaxNq] = {};
+  float w1d[kMaxNq] = {};
+};
+
+int apply_op(const OpView& op, const void* q, void* Aq, const int* skip, cudaStream_t s);
+
+// device state of one PCG run; updated by the last block of each reduction
+struct PcgState {
+  double rdotz1, rdotz2, rdotr, rdotr0, TOL, alpha, beta, pAp, tol2, zdotAp;
+  int iter, done, result, status, maxit, flexible, fixed, pad;
+};
+
+struct DeviceBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t b);
+  ~DeviceBuf();
+  template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+}  // namespace nekb
+
+struct nekb_bp {
+  nekb_bp_config cfg{};
+  int N = 0, Nq = 0, Np = 0, Nfields = 1;
+  int64_t E = 0, Nlocal = 0, offset = 0, Nmasked = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  double r1d[nekb::kMaxNq] = {}, w1d[nekb::kMaxNq] = {};
+  nekb_ogs* ogs = nullptr;
+  // geometry and basis (device)
+  nekb::DeviceBuf EX, EY, EZ, ggeo, D, Df, tri, mask, xyz;
+  nekb::DeviceBuf ggeo_f, ggeo_bf, invdeg_f;
+  // FP64 workspace: p, z, Ap, Ax, invDiag, b, r (outer residual)
+  nekb::DeviceBuf p, z, Ap, Ax, invDiag, b, rr;
+  // FP32 workspace of the inner solver
+  nekb::DeviceBuf r32, x32, p32, z32, Ap32, invDiag32, lam32;
+  // reduction scratch and solver state
+  nekb::DeviceBuf partials, counter, state;
+  nekb::PcgState* h_state = nullptr;  // pinned mirror
+  // CUDA graphs of one chunk of PCG iterations, keyed by their arguments
+  std::map<std::tuple<int, int, int, const void*, const void*, const void*, int>, cudaGraphExec_t> graphs;
+  void* net = nullptr;  // learned preconditioner in use (nekb_net*)
+  nekb::DeviceBuf net_tmp;
+};

@@ -1,0 +1,9 @@
+// axhelm instantiation: precision NEKB_FP64, Nq=12.
+#include "../axhelm_impl.cuh"
+
+namespace nekb {
+int launch_axhelm_f64_nq12(int flags, const AxArgs& a, cudaStream_t s)
+{
+  return ax::run_flags<12, NEKB_FP64>(flags, a, s);
+}
+}  // namespace nekb

@@ -1,0 +1,9 @@
+// axhelm instantiation: precision NEKB_FP32_TRILINEAR, Nq=12.
+#include "../axhelm_impl.cuh"
+
+namespace nekb {
+int launch_axhelm_tri_nq12(int flags, const AxArgs& a, cudaStream_t s)
+{
+  return ax::run_flags<12, NEKB_FP32_TRILINEAR>(flags, a, s);
+}
+}  // namespace nekb

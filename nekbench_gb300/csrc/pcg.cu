@@ -1,0 +1,749 @@
+// nekBone PCG on the device (BPPCG, nekBone/solve.cpp:44-113) and its mixed
+// precision form.
+//
+// All scalars (rdotz, rdotr, alpha, beta, TOL, the iteration counter and the
+// convergence flag) live in device memory and are updated by the last block
+// of each reduction, so an iteration needs no host round trip; the host reads
+// the state once per chunk of iterations, and each chunk is replayed as a
+// CUDA graph.  Kernels after convergence see the flag and return at once.
+//
+// Reductions are deterministic: fixed grid, fixed per-thread order, fixed
+// tree, and the final sum over block partials in block order.
+//
+// Per iteration (reference order, solve.cpp:76-109):
+//   K_p   : p = z + beta p                          (BPScaledAdd)
+//   axhelm, gather-scatter, mask : Ap = A p          (BPAxOperator)
+//   K_pAp : pAp = sum w p Ap ; alpha = rdotz/pAp     (BPWeightedInnerProduct)
+//   K_upd : x += alpha p ; r -= alpha Ap ; z = M r ; (BPUpdatePCG fused with
+//           rdotz = sum w r z ; rdotr = sum w r r     BPPreconditioner and
+//           convergence test, beta                     BPWeightedInnerProduct2)
+#include "bp.h"
+#include "nn.h"
+
+#include <cmath>
+#include <cstring>
+
+namespace nekb {
+
+namespace {
+
+constexpr int RT = 256;           // threads per reduction block
+constexpr int kMaxRedBlocks = 1216;  // 152 SMs x 8 resident blocks
+
+enum { PC_COPY = 0, PC_JACOBI = 1, PC_EXTERNAL = 2 };
+
+template <typename T>
+struct PcgArgs {
+  int64_t Nloc;
+  int64_t offset;
+  int NF;
+  const T* w;        // invDegree (Nloc)
+  const T* invDiag;  // Jacobi (Nloc) or null
+  T* r;
+  T* x;
+  T* p;
+  T* z;
+  T* Ap;
+  PcgState* st;
+  double* partials;
+  unsigned* counter;
+  double* out;       // k_wdot result
+};
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// block sum of NV values; the result is valid in thread 0
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double (*sh)[RT / 32])
+{
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    v[k] = warp_sum(v[k]);
+    if (lane == 0) sh[k][warp] = v[k];
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      double t = lane < RT / 32 ? sh[k][lane] : 0.0;
+      v[k] = warp_sum(t);
+    }
+  }
+  __syncthreads();
+}
+
+// block partial -> partials[k*gridDim + b]; returns true in the last block,
+// whose thread 0 then holds the totals in v (summed in block order).
+template <int NV>
+__device__ bool grid_sum(double (&v)[NV], double* partials, unsigned* counter)
+{
+  __shared__ double sh[NV][RT / 32];
+  __shared__ unsigned s_last;
+  block_sum<NV>(v, sh);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) partials[k * gridDim.x + blockIdx.x] = v[k];
+    __threadfence();
+    s_last = (atomicAdd(counter, 1u) == gridDim.x - 1) ? 1u : 0u;
+  }
+  __syncthreads();
+  if (s_last == 0) return false;
+  __threadfence();
+  double t[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) t[k] = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += RT)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) t[k] += __ldcg(&partials[k * gridDim.x + b]);
+  block_sum<NV>(t, sh);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = t[k];
+    *counter = 0u;
+  }
+  return threadIdx.x == 0;
+}
+
+// convergence test and beta after the (r,z) inner products (solve.cpp:77-98)
+__device__ void state_after_rz(PcgState* st, double rz, double rr, double zAp)
+{
+  const int it = ++st->iter;
+  if (it > st->maxit) {
+    st->done = 1;
+    st->result = st->maxit;
+    if (!st->fixed) st->status = NEKB_ERR_NOT_CONVERGED;
+    return;
+  }
+  st->rdotz2 = st->rdotz1;
+  st->rdotz1 = rz;
+  st->rdotr = rr;
+  if (it == 1) {
+    st->rdotr0 = rr;
+    st->TOL = fmax(st->tol2 * rr, st->tol2);
+  }
+  if (rr <= st->TOL && !st->fixed) {
+    st->done = 1;
+    st->result = it - 1;
+    return;
+  }
+  double beta;
+  if (st->flexible)
+    beta = -st->alpha * zAp / st->rdotz2;
+  else
+    beta = (it == 1) ? 0.0 : st->rdotz1 / st->rdotz2;
+  if (!isfinite(beta) || !isfinite(rr)) {
+    st->done = 1;
+    st->result = it - 1;
+    st->status = NEKB_ERR_BREAKDOWN;
+    return;
+  }
+  st->zdotAp = zAp;
+  st->beta = beta;
+}
+
+// [x += alpha p; r -= alpha Ap;] z = M r; sums w r z, w r r (, w z Ap)
+template <typename T, int MODE, bool UPDATE, bool FLEX>
+__global__ void __launch_bounds__(RT) k_update_rz(PcgArgs<T> a)
+{
+  PcgState* st = a.st;
+  if (st->done) return;
+  const T alpha = UPDATE ? (T)st->alpha : T(0);
+  T rz = 0, rr = 0, za = 0;
+  const int64_t stride = (int64_t)gridDim.x * RT;
+  for (int f = 0; f < a.NF; ++f) {
+    const int64_t fo = f * a.offset;
+    for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < a.Nloc; i += stride) {
+      const int64_t n = i + fo;
+      T r = a.r[n];
+      T ap = T(0);
+      if (UPDATE || FLEX) ap = a.Ap[n];
+      if (UPDATE) {
+        a.x[n] += alpha * a.p[n];
+        r -= alpha * ap;
+        a.r[n] = r;
+      }
+      T z;
+      if (MODE == PC_COPY) {
+        z = r;
+      } else if (MODE == PC_JACOBI) {
+        z = a.invDiag[i] * r;
+        a.z[n] = z;
+      } else {
+        z = a.z[n];
+      }
+      const T w = a.w[i];
+      rz += w * r * z;
+      rr += w * r * r;
+      if (FLEX) za += w * z * ap;
+    }
+  }
+  double v[3] = {(double)rz, (double)rr, (double)za};
+  if (grid_sum<3>(v, a.partials, a.counter)) state_after_rz(st, v[0], v[1], v[2]);
+}
+
+// x += alpha p ; r -= alpha Ap (external preconditioner path)
+template <typename T>
+__global__ void __launch_bounds__(RT) k_update(PcgArgs<T> a)
+{
+  if (a.st->done) return;
+  const T alpha = (T)a.st->alpha;
+  const int64_t N = a.NF * a.offset;
+  for (int64_t n = (int64_t)blockIdx.x * RT + threadIdx.x; n < N; n += (int64_t)gridDim.x * RT) {
+    a.x[n] += alpha * a.p[n];
+    a.r[n] -= alpha * a.Ap[n];
+  }
+}
+
+// p = z + beta p   (z = r for the COPY preconditioner)
+template <typename T, int MODE>
+__global__ void __launch_bounds__(RT) k_pupdate(PcgArgs<T> a)
+{
+  if (a.st->done) return;
+  const T beta = (T)a.st->beta;
+  const T* zs = (MODE == PC_COPY) ? a.r : a.z;
+  const int64_t N = a.NF * a.offset;
+  for (int64_t n = (int64_t)blockIdx.x * RT + threadIdx.x; n < N; n += (int64_t)gridDim.x * RT)
+    a.p[n] = zs[n] + beta * a.p[n];
+}
+
+// pAp = sum w p Ap ; alpha = rdotz / pAp
+template <typename T>
+__global__ void __launch_bounds__(RT) k_pap(PcgArgs<T> a)
+{
+  PcgState* st = a.st;
+  if (st->done) return;
+  T acc = 0;
+  const int64_t stride = (int64_t)gridDim.x * RT;
+  for (int f = 0; f < a.NF; ++f) {
+    const int64_t fo = f * a.offset;
+    for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < a.Nloc; i += stride)
+      acc += a.w[i] * a.p[i + fo] * a.Ap[i + fo];
+  }
+  double v[1] = {(double)acc};
+  if (grid_sum<1>(v, a.partials, a.counter)) {
+    const double pAp = v[0];
+    const double alpha = st->rdotz1 / pAp;
+    st->pAp = pAp;
+    if (!(pAp > 0.0) || !isfinite(alpha)) {
+      st->done = 1;
+      st->result = st->iter - 1;
+      st->status = NEKB_ERR_BREAKDOWN;
+      return;
+    }
+    st->alpha = alpha;
+  }
+}
+
+// out = sum w a b over fields
+template <typename T>
+__global__ void __launch_bounds__(RT) k_wdot(PcgArgs<T> a, const T* u, const T* v2)
+{
+  T acc = 0;
+  const int64_t stride = (int64_t)gridDim.x * RT;
+  for (int f = 0; f < a.NF; ++f) {
+    const int64_t fo = f * a.offset;
+    for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < a.Nloc; i += stride)
+      acc += a.w[i] * u[i + fo] * v2[i + fo];
+  }
+  double v[1] = {(double)acc};
+  if (grid_sum<1>(v, a.partials, a.counter)) *a.out = v[0];
+}
+
+// y = alpha x + beta y
+template <typename T>
+__global__ void k_axpby(int64_t N, T alpha, const T* x, T beta, T* y)
+{
+  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x)
+    y[n] = alpha * x[n] + beta * y[n];
+}
+
+// r = b - Ax (FP64)
+__global__ void k_residual(int64_t N, const double* b, const double* Ax, double* r)
+{
+  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x)
+    r[n] = b[n] - Ax[n];
+}
+
+// r32 = float(s * r64)
+__global__ void k_scale_down(int64_t N, double s, const double* r, float* r32)
+{
+  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x)
+    r32[n] = (float)(s * r[n]);
+}
+
+// x64 += s * x32
+__global__ void k_correct(int64_t N, double s, const float* x32, double* x)
+{
+  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x)
+    x[n] += s * (double)x32[n];
+}
+
+// mask list entries set to a value (updateJacobi's mapB==1 nodes, updateJacobi.okl:77-79)
+__global__ void k_mask_set(int64_t Nm, const int32_t* ids, double v, double* q)
+{
+  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < Nm; n += (int64_t)gridDim.x * blockDim.x)
+    q[ids[n]] = v;
+}
+
+__global__ void k_d2f_scaled(int64_t N, const double* a, float* b)
+{
+  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x)
+    b[n] = (float)a[n];
+}
+
+inline unsigned red_grid(int64_t n)
+{
+  int64_t b = (n + RT - 1) / RT;
+  if (b < 1) b = 1;
+  if (b > kMaxRedBlocks) b = kMaxRedBlocks;
+  return (unsigned)b;
+}
+
+inline unsigned vec_grid(int64_t n)
+{
+  int64_t b = (n + RT - 1) / RT;
+  if (b < 1) b = 1;
+  if (b > 152 * 16) b = 152 * 16;
+  return (unsigned)b;
+}
+
+// the external (learned) preconditioner: z = M(r), launched on the stream
+struct ExtPrecond {
+  nekb_bp* bp = nullptr;
+  nekb_net* net = nullptr;
+  const float* invDiag = nullptr;
+  const float* w = nullptr;
+};
+
+template <typename T>
+int launch_iteration(const OpView& op, PcgArgs<T> a, int mode, bool flex, const ExtPrecond* ext,
+                     cudaStream_t s)
+{
+  const int64_t Nall = a.NF * a.offset;
+  const unsigned vg = vec_grid(Nall), rg = red_grid(a.Nloc);
+  if (mode == PC_COPY)
+    k_pupdate<T, PC_COPY><<<vg, RT, 0, s>>>(a);
+  else
+    k_pupdate<T, PC_JACOBI><<<vg, RT, 0, s>>>(a);
+  NEKB_CUDA(cudaGetLastError());
+  NEKB_TRY(apply_op(op, a.p, a.Ap, &a.st->done, s));
+  k_pap<T><<<rg, RT, 0, s>>>(a);
+  NEKB_CUDA(cudaGetLastError());
+  if (mode == PC_EXTERNAL) {
+    k_update<T><<<vg, RT, 0, s>>>(a);
+    NEKB_CUDA(cudaGetLastError());
+    if constexpr (sizeof(T) == 4) {
+      NEKB_TRY(net_precondition(ext->bp, ext->net, a.r, a.z, ext->invDiag, ext->w, &a.st->done, s));
+    } else {
+      return fail(NEKB_ERR_UNSUPPORTED, "learned preconditioner runs in FP32 only");
+    }
+    if (flex)
+      k_update_rz<T, PC_EXTERNAL, false, true><<<rg, RT, 0, s>>>(a);
+    else
+      k_update_rz<T, PC_EXTERNAL, false, false><<<rg, RT, 0, s>>>(a);
+  } else if (mode == PC_JACOBI) {
+    if (flex)
+      k_update_rz<T, PC_JACOBI, true, true><<<rg, RT, 0, s>>>(a);
+    else
+      k_update_rz<T, PC_JACOBI, true, false><<<rg, RT, 0, s>>>(a);
+  } else {
+    if (flex)
+      k_update_rz<T, PC_COPY, true, true><<<rg, RT, 0, s>>>(a);
+    else
+      k_update_rz<T, PC_COPY, true, false><<<rg, RT, 0, s>>>(a);
+  }
+  NEKB_CUDA(cudaGetLastError());
+  return NEKB_OK;
+}
+
+template <typename T>
+int launch_first_rz(PcgArgs<T> a, int mode, bool flex, const ExtPrecond* ext, cudaStream_t s)
+{
+  const unsigned rg = red_grid(a.Nloc);
+  if (mode == PC_EXTERNAL) {
+    if constexpr (sizeof(T) == 4) {
+      NEKB_TRY(net_precondition(ext->bp, ext->net, a.r, a.z, ext->invDiag, ext->w, &a.st->done, s));
+    }
+    if (flex)
+      k_update_rz<T, PC_EXTERNAL, false, true><<<rg, RT, 0, s>>>(a);
+    else
+      k_update_rz<T, PC_EXTERNAL, false, false><<<rg, RT, 0, s>>>(a);
+  } else if (mode == PC_JACOBI) {
+    if (flex)
+      k_update_rz<T, PC_JACOBI, false, true><<<rg, RT, 0, s>>>(a);
+    else
+      k_update_rz<T, PC_JACOBI, false, false><<<rg, RT, 0, s>>>(a);
+  } else {
+    if (flex)
+      k_update_rz<T, PC_COPY, false, true><<<rg, RT, 0, s>>>(a);
+    else
+      k_update_rz<T, PC_COPY, false, false><<<rg, RT, 0, s>>>(a);
+  }
+  NEKB_CUDA(cudaGetLastError());
+  return NEKB_OK;
+}
+
+template <typename T>
+int wdot(nekb_bp* bp, const T* w, const T* u, const T* v, int NF, double* result)
+{
+  PcgArgs<T> a{};
+  a.Nloc = bp->Nlocal;
+  a.offset = bp->offset;
+  a.NF = NF;
+  a.w = w;
+  a.partials = bp->partials.as<double>();
+  a.counter = bp->counter.as<unsigned>() + 4;
+  a.out = bp->partials.as<double>() + 3 * 4096;
+  k_wdot<T><<<red_grid(a.Nloc), RT, 0, bp->stream>>>(a, u, v);
+  NEKB_CUDA(cudaGetLastError());
+  NEKB_CUDA(cudaMemcpyAsync(result, a.out, sizeof(double), cudaMemcpyDeviceToHost, bp->stream));
+  NEKB_CUDA(cudaStreamSynchronize(bp->stream));
+  return NEKB_OK;
+}
+
+// PCG on (r, x) with operator op.  Workspace p, z, Ap, Ax of Nfields*offset.
+template <typename T>
+int pcg_core(nekb_bp* bp, const OpView& op, T* r, T* x, const T* w, const T* invDiag, T* p, T* z,
+             T* Ap, T* Ax, int mode, bool flex, bool x_is_zero, double tol, int maxit,
+             bool fixed, int chunk, bool use_graph, const ExtPrecond* ext, int* iters, int* status,
+             double* rdotr0, double* rdotr)
+{
+  cudaStream_t s = bp->stream;
+  const int NF = op.Nfields;
+  const int64_t Nall = NF * bp->offset;
+  if (!x_is_zero) {
+    NEKB_TRY(apply_op(op, x, Ax, nullptr, s));
+    k_axpby<T><<<vec_grid(Nall), RT, 0, s>>>(Nall, T(-1), Ax, T(1), r);
+    NEKB_CUDA(cudaGetLastError());
+  }
+  NEKB_CUDA(cudaMemsetAsync(p, 0, sizeof(T) * Nall, s));
+  NEKB_CUDA(cudaMemsetAsync(Ap, 0, sizeof(T) * Nall, s));
+
+  PcgState h{};
+  h.rdotz1 = 1.0;
+  h.rdotz2 = 0.0;
+  h.alpha = 0.0;
+  h.beta = 0.0;
+  h.tol2 = tol * tol;
+  h.maxit = maxit;
+  h.flexible = flex ? 1 : 0;
+  h.fixed = fixed ? 1 : 0;
+  PcgState* st = bp->state.as<PcgState>();
+  *bp->h_state = h;
+  NEKB_CUDA(cudaMemcpyAsync(st, bp->h_state, sizeof(PcgState), cudaMemcpyHostToDevice, s));
+
+  PcgArgs<T> a{};
+  a.Nloc = bp->Nlocal;
+  a.offset = bp->offset;
+  a.NF = NF;
+  a.w = w;
+  a.invDiag = invDiag;
+  a.r = r;
+  a.x = x;
+  a.p = p;
+  a.z = z;
+  a.Ap = Ap;
+  a.st = st;
+  a.partials = bp->partials.as<double>();
+  a.counter = bp->counter.as<unsigned>();
+  NEKB_TRY(launch_first_rz<T>(a, mode, flex, ext, s));
+
+  if (chunk < 1) chunk = 1;
+  cudaGraphExec_t gexec = nullptr;
+  if (use_graph) {
+    auto key = std::make_tuple(op.precision * 64 + mode * 4 + (flex ? 2 : 0) + (int)(sizeof(T) == 8),
+                               chunk, op.flags, (const void*)op.lambda, (const void*)r, (const void*)x,
+                               (int)(ext && ext->net ? 1 : 0));
+    auto it = bp->graphs.find(key);
+    if (it != bp->graphs.end()) {
+      gexec = it->second;
+    } else {
+      // one plain launch of the operator first (p = 0, so Ap stays 0): kernel
+      // attributes are then set outside the capture
+      NEKB_TRY(apply_op(op, p, Ap, &st->done, s));
+      cudaGraph_t g = nullptr;
+      NEKB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      int st_cap = NEKB_OK;
+      for (int c = 0; c < chunk && st_cap == NEKB_OK; ++c)
+        st_cap = launch_iteration<T>(op, a, mode, flex, ext, s);
+      cudaError_t ce = cudaStreamEndCapture(s, &g);
+      if (st_cap != NEKB_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st_cap;
+      }
+      if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture", __FILE__, __LINE__);
+      ce = cudaGraphInstantiate(&gexec, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) return cuda_fail(ce, "cudaGraphInstantiate", __FILE__, __LINE__);
+      bp->graphs[key] = gexec;
+    }
+  }
+
+  const int max_chunks = (maxit + 1 + chunk - 1) / chunk + 1;
+  for (int c = 0; c < max_chunks; ++c) {
+    if (gexec) {
+      NEKB_CUDA(cudaGraphLaunch(gexec, s));
+    } else {
+      for (int k = 0; k < chunk; ++k) NEKB_TRY(launch_iteration<T>(op, a, mode, flex, ext, s));
+    }
+    NEKB_CUDA(cudaMemcpyAsync(bp->h_state, st, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
+    NEKB_CUDA(cudaStreamSynchronize(s));
+    if (bp->h_state->done) break;
+  }
+  const PcgState& hs = *bp->h_state;
+  if (!hs.done) return fail(NEKB_ERR_CUDA, "PCG: iteration state did not terminate");
+  *iters = hs.result;
+  *status = hs.status;
+  *rdotr0 = hs.rdotr0;
+  *rdotr = hs.rdotr;
+  return NEKB_OK;
+}
+
+// Homogeneous Dirichlet nodes carry no unknown: zero them in the right-hand
+// side and the initial guess so the masked operator stays symmetric.
+int mask_rhs_guess(nekb_bp* bp, double* r, double* x)
+{
+  NEKB_TRY(launch_mask(bp->Nmasked, bp->mask.as<int32_t>(), bp->Nfields, bp->offset, r,
+                       NEKB_DOUBLE, nullptr, bp->stream));
+  NEKB_TRY(launch_mask(bp->Nmasked, bp->mask.as<int32_t>(), bp->Nfields, bp->offset, x,
+                       NEKB_DOUBLE, nullptr, bp->stream));
+  return NEKB_OK;
+}
+
+int ensure_jacobi64(nekb_bp* bp, int bk, const double* lambda)
+{
+  cudaStream_t s = bp->stream;
+  double* d = bp->invDiag.as<double>();
+  NEKB_TRY(launch_update_jacobi(bp->Nq, bp->E, bp->offset, nullptr, bp->ggeo.as<double>(),
+                                bp->D.as<double>(), lambda, bk, d, s));
+  if (bp->Nmasked > 0) {
+    k_mask_set<<<vec_grid(bp->Nmasked), RT, 0, s>>>(bp->Nmasked, bp->mask.as<int32_t>(), 1.0, d);
+    NEKB_CUDA(cudaGetLastError());
+  }
+  NEKB_TRY(launch_gs_add(bp->ogs->Nmulti, bp->ogs->d_offsets, bp->ogs->d_ids, 1, bp->offset, d,
+                         NEKB_DOUBLE, nullptr, s));
+  NEKB_TRY(launch_vec_inv(d, bp->offset, s));
+  return NEKB_OK;
+}
+
+}  // namespace
+
+OpView make_op(nekb_bp* bp, int bk, int precision, const void* lambda)
+{
+  OpView op;
+  op.Nq = bp->Nq;
+  op.flags = (bk ? NEKB_AX_BK : 0) | (bp->Nfields == 3 ? NEKB_AX_N3 : 0);
+  op.precision = precision;
+  op.Nfields = bp->Nfields;
+  op.E = bp->E;
+  op.offset = bp->offset;
+  op.lambda = lambda;
+  op.ogs = bp->ogs;
+  op.mask = bp->mask.as<int32_t>();
+  op.Nmasked = bp->Nmasked;
+  for (int i = 0; i < bp->Nq; ++i) {
+    op.r1d[i] = (float)bp->r1d[i];
+    op.w1d[i] = (float)bp->w1d[i];
+  }
+  switch (precision) {
+    case NEKB_FP64: op.ggeo = bp->ggeo.p; op.D = bp->D.p; break;
+    case NEKB_FP32: op.ggeo = bp->ggeo_f.p; op.D = bp->Df.p; break;
+    case NEKB_BF16: op.ggeo = bp->ggeo_bf.p; op.D = bp->Df.p; break;
+    case NEKB_FP32_TRILINEAR: op.ggeo = bp->tri.p; op.D = bp->Df.p; break;
+  }
+  return op;
+}
+
+// lower-precision copies of geometry, lambda, weights and the Jacobi diagonal
+int prepare_inner(nekb_bp* bp, int precision, int bk, const double* lambda, bool jacobi)
+{
+  cudaStream_t s = bp->stream;
+  const int64_t Nl = bp->Nlocal;
+  const int64_t Nall = bp->Nfields * bp->offset;
+  for (DeviceBuf* w : {&bp->r32, &bp->x32, &bp->p32, &bp->z32, &bp->Ap32})
+    NEKB_TRY(w->ensure(sizeof(float) * Nall));
+  if (bp->invdeg_f.p == nullptr) {
+    NEKB_TRY(bp->invdeg_f.ensure(sizeof(float) * Nl));
+    NEKB_TRY(launch_convert_d2f(bp->ogs->d_invDegree, bp->invdeg_f.as<float>(), Nl, s));
+  }
+  if (precision == NEKB_FP32 && bp->ggeo_f.p == nullptr) {
+    NEKB_TRY(bp->ggeo_f.ensure(sizeof(float) * 7 * Nl));
+    NEKB_TRY(launch_convert_d2f(bp->ggeo.as<double>(), bp->ggeo_f.as<float>(), 7 * Nl, s));
+  }
+  if (precision == NEKB_BF16 && bp->ggeo_bf.p == nullptr) {
+    NEKB_TRY(bp->ggeo_bf.ensure(sizeof(__nv_bfloat16) * 7 * Nl));
+    NEKB_TRY(launch_convert_d2bf(bp->ggeo.as<double>(), bp->ggeo_bf.as<__nv_bfloat16>(), 7 * Nl, s));
+  }
+  if (!bk) {
+    if (lambda == nullptr) return fail(NEKB_ERR_INVALID, "PCG: lambda is NULL for a Helmholtz solve");
+    if (precision == NEKB_BF16) {
+      NEKB_TRY(bp->lam32.ensure(sizeof(__nv_bfloat16) * 2 * Nl));
+      NEKB_TRY(launch_convert_d2bf(lambda, bp->lam32.as<__nv_bfloat16>(), 2 * Nl, s));
+    } else {
+      NEKB_TRY(bp->lam32.ensure(sizeof(float) * 2 * Nl));
+      NEKB_TRY(launch_convert_d2f(lambda, bp->lam32.as<float>(), 2 * Nl, s));
+    }
+  }
+  if (jacobi) {
+    NEKB_TRY(ensure_jacobi64(bp, bk, lambda));
+    NEKB_TRY(bp->invDiag32.ensure(sizeof(float) * Nl));
+    NEKB_TRY(launch_convert_d2f(bp->invDiag.as<double>(), bp->invDiag32.as<float>(), Nl, s));
+  }
+  return NEKB_OK;
+}
+
+int solve_fp64(nekb_bp* bp, const double* lambda, double* r, double* x, double tol, int maxit,
+               const nekb_pcg_opts& o, nekb_pcg_stats* stats)
+{
+  cudaStream_t s = bp->stream;
+  const int64_t Nall = bp->Nfields * bp->offset;
+  if (!o.bk && lambda == nullptr) return fail(NEKB_ERR_INVALID, "PCG: lambda is NULL for a Helmholtz solve");
+  if (o.precond == NEKB_PRECOND_LEARNED) return fail(NEKB_ERR_UNSUPPORTED, "learned preconditioner needs the mixed solver");
+  OpView op = make_op(bp, o.bk, NEKB_FP64, lambda);
+  NEKB_TRY(bp->b.ensure(sizeof(double) * Nall));
+  NEKB_TRY(bp->rr.ensure(sizeof(double) * Nall));
+  NEKB_TRY(mask_rhs_guess(bp, r, x));
+  NEKB_CUDA(cudaMemcpyAsync(bp->b.p, r, sizeof(double) * Nall, cudaMemcpyDeviceToDevice, s));
+  const int mode = o.precond == NEKB_PRECOND_JACOBI ? PC_JACOBI : PC_COPY;
+  if (mode == PC_JACOBI) NEKB_TRY(ensure_jacobi64(bp, o.bk, lambda));
+  int iters = 0, status = 0;
+  double rdotr0 = 0, rdotr = 0;
+  NEKB_TRY(pcg_core<double>(bp, op, r, x, bp->ogs->d_invDegree, bp->invDiag.as<double>(),
+                            bp->p.as<double>(), bp->z.as<double>(), bp->Ap.as<double>(),
+                            bp->Ax.as<double>(), mode, o.flexible != 0, false, tol, maxit,
+                            o.fixed_iterations != 0, o.check_every, o.use_graph != 0, nullptr,
+                            &iters, &status, &rdotr0, &rdotr));
+  // true FP64 residual |b - A x|_w / |b - A x0|_w
+  NEKB_TRY(apply_op(op, x, bp->Ax.p, nullptr, s));
+  k_residual<<<vec_grid(Nall), RT, 0, s>>>(Nall, bp->b.as<double>(), bp->Ax.as<double>(), bp->rr.as<double>());
+  NEKB_CUDA(cudaGetLastError());
+  double tr = 0;
+  NEKB_TRY(wdot<double>(bp, bp->ogs->d_invDegree, bp->rr.as<double>(), bp->rr.as<double>(), bp->Nfields, &tr));
+  stats->iterations = iters;
+  stats->outer_iterations = 1;
+  stats->status = status;
+  stats->rdotr0 = rdotr0;
+  stats->rdotr = rdotr;
+  stats->true_rel_res = rdotr0 > 0 ? std::sqrt(tr / rdotr0) : std::sqrt(tr);
+  return NEKB_OK;
+}
+
+// FP64 iterative refinement around an FP32 / BF16 inner PCG:
+//   r = b - A64 x ; while |r|_w > tol |r0|_w : solve A32 d = r/|r| ; x += |r| d
+int solve_mixed(nekb_bp* bp, const double* lambda, double* r, double* x, double tol, int maxit,
+                const nekb_pcg_opts& o, nekb_pcg_stats* stats)
+{
+  cudaStream_t s = bp->stream;
+  const int64_t Nall = bp->Nfields * bp->offset;
+  const int prec = o.inner_precision;
+  if (prec != NEKB_FP32 && prec != NEKB_BF16 && prec != NEKB_FP32_TRILINEAR)
+    return fail(NEKB_ERR_INVALID, "mixed solver: inner precision %d", prec);
+  if (!o.bk && lambda == nullptr) return fail(NEKB_ERR_INVALID, "PCG: lambda is NULL for a Helmholtz solve");
+  const bool learned = o.precond == NEKB_PRECOND_LEARNED;
+  const bool jacobi = o.precond == NEKB_PRECOND_JACOBI || learned;
+  if (learned && o.net == nullptr) return fail(NEKB_ERR_INVALID, "learned preconditioner: net is NULL");
+  NEKB_TRY(prepare_inner(bp, prec, o.bk, lambda, jacobi));
+  OpView op64 = make_op(bp, o.bk, NEKB_FP64, lambda);
+  OpView op32 = make_op(bp, o.bk, prec, o.bk ? nullptr : bp->lam32.p);
+  NEKB_TRY(bp->b.ensure(sizeof(double) * Nall));
+  NEKB_TRY(bp->rr.ensure(sizeof(double) * Nall));
+  double* b = bp->b.as<double>();
+  NEKB_TRY(mask_rhs_guess(bp, r, x));
+  NEKB_CUDA(cudaMemcpyAsync(b, r, sizeof(double) * Nall, cudaMemcpyDeviceToDevice, s));
+  // r = b - A x
+  NEKB_TRY(apply_op(op64, x, bp->Ax.p, nullptr, s));
+  k_residual<<<vec_grid(Nall), RT, 0, s>>>(Nall, b, bp->Ax.as<double>(), r);
+  NEKB_CUDA(cudaGetLastError());
+  double rdotr0 = 0;
+  NEKB_TRY(wdot<double>(bp, bp->ogs->d_invDegree, r, r, bp->Nfields, &rdotr0));
+  const double TOL = std::fmax(tol * tol * rdotr0, tol * tol);
+  double rdotr = rdotr0;
+  int total = 0, outer = 0, status = NEKB_OK;
+  const int max_outer = o.max_outer > 0 ? o.max_outer : 20;
+  const double inner_tol = o.inner_tol > 0 ? o.inner_tol : 1e-3;
+  ExtPrecond ext;
+  ext.bp = bp;
+  ext.net = (nekb_net*)o.net;
+  ext.invDiag = bp->invDiag32.as<float>();
+  ext.w = bp->invdeg_f.as<float>();
+  const int mode = learned ? PC_EXTERNAL : (jacobi ? PC_JACOBI : PC_COPY);
+  while (rdotr > TOL && outer < max_outer) {
+    const double nr = std::sqrt(rdotr);
+    k_scale_down<<<vec_grid(Nall), RT, 0, s>>>(Nall, 1.0 / nr, r, bp->r32.as<float>());
+    NEKB_CUDA(cudaGetLastError());
+    NEKB_CUDA(cudaMemsetAsync(bp->x32.p, 0, sizeof(float) * Nall, s));
+    int it = 0, st = 0;
+    double a0 = 0, a1 = 0;
+    NEKB_TRY(pcg_core<float>(bp, op32, bp->r32.as<float>(), bp->x32.as<float>(),
+                             bp->invdeg_f.as<float>(), bp->invDiag32.as<float>(),
+                             bp->p32.as<float>(), bp->z32.as<float>(), bp->Ap32.as<float>(),
+                             bp->Ap32.as<float>(), mode, learned || o.flexible != 0, true,
+                             inner_tol, maxit, false, o.check_every, o.use_graph != 0, &ext, &it,
+                             &st, &a0, &a1));
+    total += it;
+    outer++;
+    if (st == NEKB_ERR_BREAKDOWN) status = st;
+    k_correct<<<vec_grid(Nall), RT, 0, s>>>(Nall, nr, bp->x32.as<float>(), x);
+    NEKB_CUDA(cudaGetLastError());
+    NEKB_TRY(apply_op(op64, x, bp->Ax.p, nullptr, s));
+    k_residual<<<vec_grid(Nall), RT, 0, s>>>(Nall, b, bp->Ax.as<double>(), r);
+    NEKB_CUDA(cudaGetLastError());
+    NEKB_TRY(wdot<double>(bp, bp->ogs->d_invDegree, r, r, bp->Nfields, &rdotr));
+    if (status == NEKB_ERR_BREAKDOWN || it == 0) break;
+  }
+  if (rdotr > TOL && status == NEKB_OK) status = NEKB_ERR_NOT_CONVERGED;
+  stats->iterations = total;
+  stats->outer_iterations = outer;
+  stats->status = status;
+  stats->rdotr0 = rdotr0;
+  stats->rdotr = rdotr;
+  stats->true_rel_res = rdotr0 > 0 ? std::sqrt(rdotr / rdotr0) : std::sqrt(rdotr);
+  return NEKB_OK;
+}
+
+int bp_pcg(nekb_bp* bp, const double* lambda, double* r, double* x, double tol, int maxit,
+           const nekb_pcg_opts* opts, nekb_pcg_stats* stats)
+{
+  nekb_pcg_opts o;
+  if (opts) {
+    o = *opts;
+  } else {
+    std::memset(&o, 0, sizeof(o));
+    o.precond = NEKB_PRECOND_JACOBI;
+    o.check_every = 16;
+    o.use_graph = 1;
+  }
+  if (!bp || !r || !x || !stats) return fail(NEKB_ERR_INVALID, "PCG: NULL argument");
+  if (maxit < 0 || !(tol >= 0)) return fail(NEKB_ERR_INVALID, "PCG: maxit=%d tol=%g", maxit, tol);
+  if (o.check_every <= 0) o.check_every = 16;
+  cudaEvent_t e0, e1;
+  NEKB_CUDA(cudaEventCreate(&e0));
+  NEKB_CUDA(cudaEventCreate(&e1));
+  NEKB_CUDA(cudaEventRecord(e0, bp->stream));
+  int st;
+  if (o.solver == NEKB_SOLVER_MIXED)
+    st = solve_mixed(bp, lambda, r, x, tol, maxit, o, stats);
+  else
+    st = solve_fp64(bp, lambda, r, x, tol, maxit, o, stats);
+  cudaEventRecord(e1, bp->stream);
+  cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st == NEKB_OK) stats->elapsed_s = ms * 1e-3;
+  return st;
+}
+
+int bp_wdot(nekb_bp* bp, const double* u, const double* v, double* out)
+{
+  return wdot<double>(bp, bp->ogs->d_invDegree, u, v, bp->Nfields, out);
+}
+
+}  // namespace nekb

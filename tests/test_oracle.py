@@ -1,0 +1,248 @@
+"""CPU tests of the oracle (no GPU): pinned to golden vectors produced by the
+reference's own CPU code (tests/golden/make_golden.py) and, where oracle/_ref
+was built here, to that code directly; plus the reference's known-answer
+checks and properties of the basis, mesh, gather-scatter, PCG and network."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.mark.parametrize("case", ["axhelm_n3", "axhelm_n7", "axhelm_n9"])
+def test_axhelm_matches_reference_golden(case):
+    g = np.load(os.path.join(GOLD, case + ".npz"))
+    N, E = int(g["N"]), int(g["E"])
+    Nq = N + 1
+    L = E * Nq ** 3
+    for variant in range(4):
+        nf = 3 if variant & 2 else 1
+        got = O.axhelm(Nq, E, L, variant, g["ggeo"], g["D"], g["lam"], g["q"][: nf * L].copy())
+        # same loop structure and operation order as kernel/CPU/axhelm.c: bit-identical
+        assert np.array_equal(got, g[f"Aq_cpu_v{variant}"]), variant
+    # axhelmReference.cpp uses a scalar lambda (lambda0 = 1)
+    for lam1 in (0.0, 1.1):
+        lam = np.concatenate([np.ones(L), lam1 * np.ones(L)])
+        flags = O.AX_BK if lam1 == 0.0 else 0
+        got = O.axhelm(Nq, E, L, flags, g["ggeo"], g["D"], lam, g["q"][:L].copy())
+        assert rel(got, g[f"Aq_reference_lam{lam1}"]) < 1e-14
+
+
+def test_uniform_generator_golden():
+    g = np.load(os.path.join(GOLD, "uniform.npz"))
+    assert np.array_equal(O.uniform(16, 5, 2), g["u_seed5_stream2"])
+    assert np.array_equal(O.uniform(16, 0, 0), g["u_seed0_stream0"])
+
+
+def test_weighted_inner_product_golden():
+    g = np.load(os.path.join(GOLD, "weighted_inner_product.npz"))
+    w, a, b = g["w"], g["a"], g["b"]
+    n = len(w)
+    L = O.lib()
+    L.nekbo_wdot.restype = __import__("ctypes").c_double
+    ab = L.nekbo_wdot(n, 1, n, w.ctypes.data, a.ctypes.data, b.ctypes.data)
+    aa = L.nekbo_wdot(n, 1, n, w.ctypes.data, a.ctypes.data, a.ctypes.data)
+    # weightedInnerProductUpdate (CPU/weightedInnerProduct.c:64): [sum w a b, sum w a a]
+    assert rel(np.array([ab, aa]), g["wab"]) < 1e-13
+
+
+@pytest.mark.parametrize("N", [7, 9, 3])
+def test_live_reference_when_built(N):
+    R = O.ref(N + 1)
+    if R is None:
+        pytest.skip("oracle/_ref not built (reference sources absent)")
+    m = O.BoxMesh(N, 3, 2, 2, perturb=0.1, seed=N)
+    E, L = m.E, m.Nlocal
+    lam = np.concatenate([O.uniform(L, 1, 1, 0.5, 1.5), O.uniform(L, 1, 2, 0.5, 2.0)])
+    q = O.uniform(3 * L, 1, 3, -1, 1)
+    for variant in range(4):
+        nf = 3 if variant & 2 else 1
+        ref = np.zeros(nf * L)
+        R.nekref_axhelm_cpu(variant, E, L, m.ggeo, m.D, lam.ctypes.data, q[: nf * L].copy(), ref)
+        got = O.axhelm(N + 1, E, L, variant, m.ggeo, m.D, lam, q[: nf * L].copy())
+        assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("N", range(1, 12))
+def test_gll_basis(N):
+    x, w = O.gll(N)
+    assert x[0] == -1 and x[-1] == 1 and np.all(np.diff(x) > 0)
+    assert np.array_equal(x, -x[::-1])
+    D = O.dmatrix(x).reshape(N + 1, N + 1)
+    for p in range(N + 1):  # D differentiates polynomials of degree <= N exactly
+        f, df = x ** p, (p * x ** (p - 1) if p else 0 * x)
+        assert np.abs(D @ f - df).max() < 1e-11 * (1 + np.abs(df).max())
+    for p in range(2 * N):  # GLL quadrature is exact to degree 2N-1
+        exact = (1 - (-1) ** (p + 1)) / (p + 1)
+        assert abs(np.dot(w, x ** p) - exact) < 1e-13
+    # centro-antisymmetry of D on symmetric nodes
+    assert np.abs(D + D[::-1, ::-1]).max() < 1e-12
+
+
+@pytest.mark.parametrize("N", [0, 1, 4, 7, 9])
+def test_gauss_basis(N):
+    x, w = O.gauss(N)
+    for p in range(2 * N + 2):
+        exact = (1 - (-1) ** (p + 1)) / (p + 1)
+        assert abs(np.dot(w, x ** p) - exact) < 1e-13
+
+
+def test_affine_box_geometric_factors():
+    """Unperturbed box: G = JW*diag(1/hr^2), G01=G02=G12=0, JW = J w_i w_j w_k."""
+    N, nx, ny, nz = 4, 2, 3, 5
+    m = O.BoxMesh(N, nx, ny, nz, perturb=0.0)
+    Np = m.Np
+    x, w = O.gll(N)
+    W = np.einsum("k,j,i->kji", w, w, w).ravel()
+    hx, hy, hz = 1 / nx / 2, 1 / ny / 2, 1 / nz / 2  # d x / d r
+    J = hx * hy * hz
+    g = m.ggeo.reshape(m.E, 7, Np)
+    assert np.abs(g[:, 0] - J * W).max() < 1e-15
+    assert np.abs(g[:, 1] - J * W / hx ** 2).max() < 1e-12
+    assert np.abs(g[:, 4] - J * W / hy ** 2).max() < 1e-12
+    assert np.abs(g[:, 6] - J * W / hz ** 2).max() < 1e-12
+    assert np.abs(g[:, [2, 3, 5]]).max() < 1e-13
+
+
+def test_perturbed_mesh_is_valid_and_watertight():
+    m = O.BoxMesh(7, 4, 4, 4, perturb=0.1, seed=2)
+    assert np.all(m.ggeo.reshape(m.E, 7, m.Np)[:, 0] > 0)  # positive Jacobian
+    # coincident nodes (same global id) have the same coordinates
+    ids = m.ids
+    nz = ids > 0
+    order = np.argsort(ids[nz], kind="stable")
+    xs = np.stack([m.x[nz], m.y[nz], m.z[nz]], 1)[order]
+    same = np.diff(ids[nz][order]) == 0
+    assert np.abs(xs[1:][same] - xs[:-1][same]).max() < 1e-14
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_ogs_known_answer(periodic):
+    """gs/main.cpp:136-193: sum(nearbyint(gs(1/gs(1)))) == number of nodes."""
+    m = O.BoxMesh(5, 3, 3, 2, periodic=periodic, dirichlet=not periodic)
+    Ng, offs, gids, invdeg = O.ogs_setup(m.ids)
+    q = np.ones(m.Nlocal)
+    O.gs_many_add(Ng, offs, gids, q)
+    q = 1 / q
+    O.gs_many_add(Ng, offs, gids, q)
+    assert int(np.rint(q).sum()) == m.Nlocal
+    assert np.allclose(invdeg[m.ids > 0] * np.bincount(m.ids)[m.ids[m.ids > 0]], 1.0)
+
+
+def test_ogs_csr_order():
+    rng = np.random.default_rng(3)
+    ids = rng.integers(0, 40, size=300).astype(np.int64)
+    Ng, offs, gids, invdeg = O.ogs_setup(ids)
+    nz = np.flatnonzero(ids)
+    assert offs[-1] == len(nz) and sorted(gids) == list(nz)
+    firsts = [gids[offs[g]] for g in range(Ng)]
+    assert firsts == sorted(firsts)  # groups numbered by first local appearance
+    for g in range(Ng):
+        mem = gids[offs[g]:offs[g + 1]]
+        assert np.all(np.diff(mem) > 0) and len(set(ids[mem])) == 1
+        assert np.all(invdeg[mem] == 1.0 / len(mem))
+    assert np.all(invdeg[ids == 0] == 1.0)
+
+
+def _problem(N=3, n=3, seed=4):
+    m = O.BoxMesh(N, n, n, n, perturb=0.1, seed=seed)
+    L = m.Nlocal
+    lam = np.concatenate([O.uniform(L, seed, 1, 0.5, 1.5), O.uniform(L, seed, 2, 0.5, 2.0)])
+    bp = O.BP(m, lam)
+    f = O.uniform(L, seed, 3, -1, 1)
+    O.gs_many_add(bp.Ng, bp.offs, bp.gids, f)
+    O.lib().nekbo_mask(len(m.maskIds), m.maskIds, f)
+    return m, bp, f
+
+
+def test_assembled_operator_is_spd():
+    m, bp, f = _problem()
+    w = bp.invdeg
+    u = O.uniform(m.Nlocal, 9, 1, -1, 1)
+    v = O.uniform(m.Nlocal, 9, 2, -1, 1)
+    for a in (u, v):
+        O.gs_many_add(bp.Ng, bp.offs, bp.gids, a)
+        a *= w  # continuous fields: average the element copies
+        O.gs_many_add(bp.Ng, bp.offs, bp.gids, a)
+        O.lib().nekbo_mask(len(m.maskIds), m.maskIds, a)
+    Au, Av = bp.apply(u), bp.apply(v)
+    s1, s2 = np.sum(w * u * Av), np.sum(w * Au * v)
+    assert abs(s1 - s2) < 1e-12 * abs(s1)
+    assert np.sum(w * u * Au) > 0
+
+
+def test_pcg_converges_and_jacobi_helps():
+    m, bp, f = _problem()
+    x1, r1 = np.zeros_like(f), f.copy()
+    it_j, hist = bp.pcg(r1, x1, 1e-8, 500, precond=1, hist=True)
+    x0, r0 = np.zeros_like(f), f.copy()
+    it_c = bp.pcg(r0, x0, 1e-8, 500, precond=0)
+    assert 0 < it_j < it_c < 500
+    assert hist[it_j] <= max(1e-16 * hist[0], 1e-16)
+    res = f - bp.apply(x1)
+    w = bp.invdeg
+    assert np.sqrt(np.sum(w * res * res) / np.sum(w * f * f)) < 1.01e-8
+    # flexible beta gives the same iterates for a fixed preconditioner
+    x2, r2 = np.zeros_like(f), f.copy()
+    it_f = bp.pcg(r2, x2, 1e-8, 500, precond=1, flexible=True)
+    assert abs(it_f - it_j) <= 1 and rel(x2, x1) < 1e-6
+
+
+def _net_forward(Nq, W, x, C):
+    o2, o3 = 27 * C, 27 * C + 27 * C * C
+    z1 = O.conv3d_forward(Nq, W[:o2], x, 1, C)
+    a1 = O.gelu(z1)
+    z2 = O.conv3d_forward(Nq, W[o2:o3], a1, C, C)
+    a2 = O.gelu(z2)
+    y = O.conv3d_forward(Nq, W[o3:], a2, C, 1)
+    return y, (z1, a1, z2, a2)
+
+
+def net_loss_grad(Nq, W, x, t, C):
+    """loss = mean (net(x) - t)^2 and its gradient, composed from the oracle layers."""
+    o2, o3 = 27 * C, 27 * C + 27 * C * C
+    y, (z1, a1, z2, a2) = _net_forward(Nq, W, x, C)
+    d = y.astype(np.float64) - t
+    loss = np.mean(d * d)
+    gy = (2 * d / d.size).astype(np.float32)
+    ga2, gW3 = O.conv3d_backward(Nq, W[o3:], a2, gy, C, 1)
+    gz2 = O.gelu_backward(z2, ga2)
+    ga1, gW2 = O.conv3d_backward(Nq, W[o2:o3], a1, gz2, C, C)
+    gz1 = O.gelu_backward(z1, ga1)
+    _, gW1 = O.conv3d_backward(Nq, W[:o2], x, gz1, 1, C, want_gin=False)
+    return loss, np.concatenate([gW1, gW2, gW3])
+
+
+def test_network_gradient_by_finite_differences():
+    Nq, C, E = 4, 4, 3
+    P = 27 * C * (C + 2)
+    rng = np.random.default_rng(1)
+    W = (rng.standard_normal(P) * 0.3).astype(np.float32)
+    x = rng.standard_normal(E * Nq ** 3).astype(np.float32)
+    t = rng.standard_normal(E * Nq ** 3).astype(np.float32)
+    loss, g = net_loss_grad(Nq, W, x, t, C)
+    for p in rng.choice(P, 25, replace=False):
+        h = 1e-2
+        Wp, Wm = W.copy(), W.copy()
+        Wp[p] += h
+        Wm[p] -= h
+        lp = np.mean((_net_forward(Nq, Wp, x, C)[0].astype(np.float64) - t) ** 2)
+        lm = np.mean((_net_forward(Nq, Wm, x, C)[0].astype(np.float64) - t) ** 2)
+        fd = (lp - lm) / (2 * h)
+        assert abs(fd - g[p]) < 2e-3 * (abs(fd) + 1e-2), (p, fd, g[p])
+
+
+def test_gelu_oracle():
+    x = np.linspace(-4, 4, 101).astype(np.float32)
+    y = O.gelu(x)
+    assert abs(y[50]) < 1e-7 and abs(y[-1] - 4 * 0.99993) < 1e-3
+    gx = O.gelu_backward(x, np.ones_like(x))
+    fd = (O.gelu(x + 1e-3) - O.gelu(x - 1e-3)) / 2e-3
+    assert np.abs(gx - fd).max() < 5e-3

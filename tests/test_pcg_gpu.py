@@ -1,0 +1,132 @@
+"""nekBone PCG on the GPU against the oracle's restatement of BPPCG
+(nekBone/solve.cpp:44-113), and the mixed-precision solver against the FP64
+true residual.  Both sides use the same mesh, geometric factors and RHS."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def T(x, dev):
+    return torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+
+
+def pair(nb, O, N, n, Nfields=1, seed=3):
+    bp = nb.BP(N, n, n, n, Nfields=Nfields, perturb=0.1, seed=seed)
+    m = O.BoxMesh(N, n, n, n, perturb=0.1, seed=seed)
+    L = bp.Nlocal
+    assert np.array_equal(bp.device_array("EX", 8 * bp.E, torch.float64).cpu().numpy(), m.EX)
+    g = bp.device_array("ggeo", 7 * L, torch.float64).cpu().numpy()
+    assert rel(g, m.ggeo) < 1e-12  # analytic trilinear map vs D applied to the nodes
+    m.ggeo = g  # identical operator on both sides
+    assert np.array_equal(bp.device_array("maskIds", bp.Nmasked, torch.int32).cpu().numpy(),
+                          m.maskIds)
+    return bp, m
+
+
+def problem(O, m, Nfields, seed, bk=False):
+    L = m.Nlocal
+    lam = np.concatenate([O.uniform(L, seed, 1, 0.5, 1.5), O.uniform(L, seed, 2, 0.5, 2.0)])
+    if bk:
+        lam = np.concatenate([np.ones(L), np.zeros(L)])
+    obp = O.BP(m, lam, bk=bk, Nfields=Nfields)
+    f = O.uniform(Nfields * L, seed, 3, -1, 1)
+    O.gs_many_add(obp.Ng, obp.offs, obp.gids, f, Nfields, L)
+    for k in range(Nfields):
+        O.lib().nekbo_mask(len(m.maskIds), m.maskIds, f[k * L:(k + 1) * L])
+    return obp, lam, f
+
+
+def true_rel_res(obp, f, x):
+    r = f - obp.apply(x)
+    w = np.tile(obp.invdeg, len(f) // len(obp.invdeg))
+    return np.sqrt(np.sum(w * r * r) / np.sum(w * f * f))
+
+
+@pytest.mark.parametrize("precond,flexible", [(1, False), (0, False), (1, True)])
+def test_fp64_pcg_matches_oracle(nb, O, dev, precond, flexible):
+    bp, m = pair(nb, O, 7, 4)
+    obp, lam, f = problem(O, m, 1, 11)
+    r_h, x_h = f.copy(), np.zeros_like(f)
+    it_o = obp.pcg(r_h, x_h, 1e-8, 500, precond=precond, flexible=flexible)
+    r_d, x_d = T(f, dev), torch.zeros(len(f), dtype=torch.float64, device=dev)
+    st = bp.pcg(T(lam, dev), r_d, x_d, 1e-8, 500, precond=precond, flexible=flexible)
+    assert st["status"] == 0
+    assert abs(st["iterations"] - it_o) <= 1, (st, it_o)
+    assert rel(x_d.cpu().numpy(), x_h) < 1e-7
+    assert st["true_rel_res"] < 1.05e-8
+    assert true_rel_res(obp, f, x_d.cpu().numpy()) < 1.05e-8
+
+
+def test_fixed_iteration_count_matches(nb, O, dev):
+    bp, m = pair(nb, O, 5, 3)
+    obp, lam, f = problem(O, m, 1, 12)
+    r_h, x_h = f.copy(), np.zeros_like(f)
+    it_o = obp.pcg(r_h, x_h, 0.0, 25, precond=1, fixed=True)
+    r_d, x_d = T(f, dev), torch.zeros(len(f), dtype=torch.float64, device=dev)
+    st = bp.pcg(T(lam, dev), r_d, x_d, 0.0, 25, fixed_iterations=True)
+    assert it_o == 25 and st["iterations"] == 25
+    assert rel(x_d.cpu().numpy(), x_h) < 1e-10
+    assert rel(r_d.cpu().numpy(), r_h) < 1e-8
+
+
+def test_three_fields_and_bk(nb, O, dev):
+    bp, m = pair(nb, O, 3, 4, Nfields=3)
+    obp, lam, f = problem(O, m, 3, 13, bk=True)
+    r_h, x_h = f.copy(), np.zeros_like(f)
+    it_o = obp.pcg(r_h, x_h, 1e-8, 400, precond=1)
+    r_d, x_d = T(f, dev), torch.zeros(len(f), dtype=torch.float64, device=dev)
+    st = bp.pcg(None, r_d, x_d, 1e-8, 400, bk=True)
+    assert abs(st["iterations"] - it_o) <= 1
+    assert rel(x_d.cpu().numpy(), x_h) < 1e-7
+
+
+def test_iteration_limit_and_graph_off(nb, O, dev):
+    bp, m = pair(nb, O, 7, 3)
+    obp, lam, f = problem(O, m, 1, 14)
+    r_d, x_d = T(f, dev), torch.zeros(len(f), dtype=torch.float64, device=dev)
+    st = bp.pcg(T(lam, dev), r_d, x_d, 1e-14, 7, use_graph=False, check_every=3)
+    assert st["iterations"] == 7 and st["status"] == nb.ERR_NOT_CONVERGED
+    r_h, x_h = f.copy(), np.zeros_like(f)
+    obp.pcg(r_h, x_h, 1e-14, 7, precond=1)
+    assert rel(x_d.cpu().numpy(), x_h) < 1e-10
+
+
+def test_zero_rhs(nb, O, dev):
+    bp, m = pair(nb, O, 3, 2)
+    L = bp.Nlocal
+    lam = torch.ones(2 * L, dtype=torch.float64, device=dev)
+    r = torch.zeros(L, dtype=torch.float64, device=dev)
+    x = torch.zeros(L, dtype=torch.float64, device=dev)
+    st = bp.pcg(lam, r, x, 1e-8, 50)
+    assert st["iterations"] == 0 and float(x.abs().max()) == 0.0
+
+
+@pytest.mark.parametrize("prec", ["FP32", "BF16", "FP32_TRILINEAR"])
+def test_mixed_precision_reaches_fp64_tolerance(nb, O, dev, prec):
+    bp, m = pair(nb, O, 7, 4)
+    obp, lam, f = problem(O, m, 1, 15)
+    r_d, x_d = T(f, dev), torch.zeros(len(f), dtype=torch.float64, device=dev)
+    st = bp.pcg(T(lam, dev), r_d, x_d, 1e-8, 1000, solver=nb.SOLVER_MIXED,
+                inner_precision=getattr(nb, prec), inner_tol=1e-3)
+    assert st["status"] == 0, st
+    assert st["true_rel_res"] <= 1e-8
+    assert true_rel_res(obp, f, x_d.cpu().numpy()) <= 1.01e-8
+    # same solution as the FP64 oracle PCG to the tolerance
+    r_h, x_h = f.copy(), np.zeros_like(f)
+    obp.pcg(r_h, x_h, 1e-11, 2000, precond=1)
+    assert rel(x_d.cpu().numpy(), x_h) < 1e-6
+
+
+def test_mixed_three_fields(nb, O, dev):
+    bp, m = pair(nb, O, 7, 3, Nfields=3)
+    obp, lam, f = problem(O, m, 3, 16)
+    r_d, x_d = T(f, dev), torch.zeros(len(f), dtype=torch.float64, device=dev)
+    st = bp.pcg(T(lam, dev), r_d, x_d, 1e-10, 1000, solver=nb.SOLVER_MIXED)
+    assert st["status"] == 0 and st["true_rel_res"] <= 1e-10
+    assert true_rel_res(obp, f, x_d.cpu().numpy()) <= 1.01e-10
