@@ -1,0 +1,427 @@
+"""Benchmark of the nekBench hot path on GB300: axhelm GDOF/s and PCG time to 1e-8.
+
+One "step" is one axhelm application (FP64, BK/Poisson, N=7) over the
+E = 64^3 = 262144-element perturbed box (134M local nodes; 9.7 GB of operands
+per step, far larger than L2, so no flush is needed between steps).  The JSON
+line also carries the PCG comparison (plain FP64 Jacobi-PCG vs FP32-inner
+mixed precision with FP64 refinement, with and without the learned
+preconditioner) to a true FP64 relative residual of 1e-8.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference's CPU axhelm (the oracle's restatement,
+bit-identical to axhelm/kernel/CPU/axhelm.c) on the host cores with all threads.
+Multi-GPU (torchrun): every rank runs the same per-GPU workload on its own
+elements (weak scaling, no collective on the data path); timing is the max
+over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "axhelm GDOF/s & PCG time-to-1e-8 (mixed+learned vs plain FP64) at N=7, 1 GB300"
+N_ORDER = 7
+V100_PUBLISHED_GDOFS = 7.41742  # axhelm/readme.md:25,31 (V100, BK, N=7)
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=50)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--n", type=int, default=64, help="elements per direction (E = n^3)")
+    p.add_argument("--pcg-n", type=int, default=64, help="elements per direction of the PCG runs")
+    p.add_argument("--no-pcg", action="store_true")
+    p.add_argument("--no-learned", action="store_true")
+    p.add_argument("--cpu-seconds", type=float, default=10.0)
+    return p.parse_args()
+
+
+# ------------------------------------------------------------------ distributed helpers
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend, rank=rank, world_size=ws)
+    return rank, ws, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(v, ws):
+    if ws <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if torch.cuda.is_available() and dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index):
+        self.index, self.proc, self.lines = index, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100", "-i", str(self.index)], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.15)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU baseline
+class CpuAxhelm:
+    """The reference's CPU axhelm (the oracle's restatement, bit-identical to
+    axhelm/kernel/CPU/axhelm.c; OpenMP over elements, all host threads) on a
+    bounded sample of the workload: n_el elements of the same N=7 perturbed box."""
+
+    def __init__(self, n_el=4096):
+        import oracle as O
+        self.O = O
+        self.m = O.BoxMesh(N_ORDER, 16, 16, max(1, n_el // 256), perturb=0.1, seed=1)
+        self.q = O.uniform(self.m.Nlocal, 1, 3, -1, 1)
+        self.Aq = np.zeros(self.m.Nlocal)
+
+    def apply(self):
+        m = self.m
+        self.O.axhelm_omp(N_ORDER + 1, m.E, m.Nlocal, self.O.AX_BK, m.ggeo, m.D, None, self.q,
+                          self.Aq)
+
+    def rate(self, seconds):
+        self.apply()  # warm-up
+        reps, t0 = 0, time.perf_counter()
+        while True:
+            self.apply()
+            reps += 1
+            el = time.perf_counter() - t0
+            if el >= seconds:
+                break
+        per = el / reps
+        return {"value": self.m.E * N_ORDER ** 3 / per / 1e9, "unit": "GDOF/s",
+                "cores": self.O.omp_threads(), "kind": "port",
+                "sample": f"{reps} applications of FP64 BK axhelm on {self.m.E} elements (N=7, "
+                          f"{self.m.Nlocal} nodes) of the same perturbed box in {el:.1f} s, "
+                          f"OpenMP over elements"}
+
+
+def run_reference(args, rank, ws):
+    if rank != 0:
+        return
+    import oracle as O
+    O.build()
+    cpu = CpuAxhelm()
+    for _ in range(args.warmup):
+        cpu.apply()
+    per_step = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        cpu.apply()
+        per_step.append(time.perf_counter() - t0)
+    med = float(np.median(per_step))
+    v = cpu.m.E * N_ORDER ** 3 / med / 1e9
+    line = {"metric": METRIC, "impl": "reference", "value": v, "unit": "GDOF/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": med * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"axhelm FP64 BK (Poisson), N=7, bounded sample of {cpu.m.E} "
+                                   f"elements of the perturbed box per step, host cores", "N": N_ORDER},
+            "cpu_baseline": {"value": v, "unit": "GDOF/s", "cores": O.omp_threads(), "kind": "port",
+                             "sample": f"{args.steps} timed applications on {cpu.m.E} elements "
+                                       f"({cpu.m.Nlocal} nodes), median"},
+            "e2e": {"value": v, "unit": "GDOF/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU arm
+def time_axhelm(nb, torch, Nq, flags, prec, E, L, g, D, lam, q, Aq, steps, warmup, stream):
+    for _ in range(warmup):
+        nb.axhelm(Nq, flags, prec, E, L, g, D, lam, q, Aq, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        nb.axhelm(Nq, flags, prec, E, L, g, D, lam, q, Aq, stream=stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def load_profile_traffic():
+    path = os.path.join(ROOT, "profiles", "axhelm_fp64_bk_n7.md")
+    if not os.path.exists(path):
+        return None
+    for ln in open(path):
+        if ln.startswith("dram_bytes_per_launch_full:"):
+            try:
+                return float(ln.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def pcg_comparison(nb, torch, dev, n, learned):
+    """Three solvers on the same problem to true FP64 relative residual 1e-8."""
+    import oracle as O
+    bp = nb.BP(N_ORDER, n, n, n, perturb=0.1, seed=5)
+    L = bp.Nlocal
+    lam = torch.empty(2 * L, dtype=torch.float64, device=dev)
+    nb.fill_uniform(lam[:L], 5, 1, 0.5, 1.5)
+    nb.fill_uniform(lam[L:], 5, 2, 0.5, 2.0)
+    f = torch.empty(L, dtype=torch.float64, device=dev)
+    nb.fill_uniform(f, 5, 3, -1.0, 1.0)
+    bp.ogs.gather_scatter_many(f)
+    torch.cuda.synchronize()
+    out = {"workload": f"N=7, E={n}^3={bp.E} perturbed box, Dirichlet, lambda0~U[0.5,1.5], "
+                       f"lambda1~U[0.5,2.0], f~U[-1,1] assembled; stop at true FP64 "
+                       f"relative residual 1e-8", "E": bp.E, "unknowns_local": L}
+    runs = [("fp64_jacobi", dict(solver=nb.SOLVER_FP64)),
+            ("mixed_fp32_trilinear", dict(solver=nb.SOLVER_MIXED, inner_precision=nb.FP32_TRILINEAR)),
+            ("mixed_bf16", dict(solver=nb.SOLVER_MIXED, inner_precision=nb.BF16))]
+    net = None
+    if learned:
+        net = learned_net(nb, torch, dev)
+        if net is not None:
+            runs.append(("mixed_learned", dict(solver=nb.SOLVER_MIXED, inner_precision=nb.FP32_TRILINEAR,
+                                               precond=nb.PRECOND_LEARNED, net=net)))
+    for name, kw in runs:
+        best = None
+        for rep in range(2):  # first run instantiates the graphs
+            r, x = f.clone(), torch.zeros_like(f)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            st = bp.pcg(lam, r, x, 1e-8, 20000, **kw)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+            st["wall_s"] = wall
+            if best is None or st["elapsed_s"] < best["elapsed_s"]:
+                best = st
+        out[name] = {k: best[k] for k in ("iterations", "outer_iterations", "status",
+                                           "true_rel_res", "elapsed_s", "wall_s")}
+    base = out["fp64_jacobi"]["elapsed_s"]
+    for name, _ in runs[1:]:
+        out[name]["speedup_vs_fp64"] = base / out[name]["elapsed_s"]
+    bp.free()
+    del bp
+    return out
+
+
+def learned_net(nb, torch, dev):
+    path = os.path.join(ROOT, "nekbench_gb300", "weights", "precond_n7_c16.bin")
+    if not os.path.exists(path) or not hasattr(nb, "Net"):
+        return None
+    return nb.Net.load(path)
+
+
+def run_gpu(args, rank, ws, local):
+    import torch
+
+    import nekbench_gb300 as nb
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(device=dev)
+    n = args.n
+    Nq = N_ORDER + 1
+    bp = nb.BP(N_ORDER, n, n, n, perturb=0.1, seed=1, stream=stream.cuda_stream)
+    E, L = bp.E, bp.Nlocal
+    g, D = bp.ptr("ggeo"), bp.ptr("D")
+    q = torch.empty(L, dtype=torch.float64, device=dev)
+    nb.fill_uniform(q, 1, 3, -1.0, 1.0, stream=stream.cuda_stream)
+    Aq = torch.empty_like(q)
+    torch.cuda.synchronize()
+
+    # ---- device-resident timing (inputs already in HBM)
+    barrier(ws)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms = time_axhelm(nb, torch, Nq, nb.AX_BK, nb.FP64, E, L, g, D, None, q, Aq, args.steps,
+                         args.warmup, stream)
+    torch.cuda.synchronize()
+    barrier(ws)
+    ms = max_over_ranks(ms, ws)
+    gdofs = ws * E * N_ORDER ** 3 / (ms * 1e-3) / 1e9
+
+    # ---- end to end through the C ABI with host buffers (q in, Aq out)
+    hq = torch.empty(L, dtype=torch.float64, pin_memory=True)
+    hq.copy_(q.cpu())
+    hA = torch.empty(L, dtype=torch.float64, pin_memory=True)
+    e2e_steps = max(3, min(args.steps, 10))
+    for i in range(e2e_steps + 2):
+        if i == 2:
+            torch.cuda.synchronize()
+            barrier(ws)
+            t0 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            q.copy_(hq, non_blocking=True)
+            nb.axhelm(Nq, nb.AX_BK, nb.FP64, E, L, g, D, None, q, Aq, stream=stream.cuda_stream)
+            hA.copy_(Aq, non_blocking=True)
+        stream.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_s = max_over_ranks(e2e_s, ws)
+    e2e_gdofs = ws * E * N_ORDER ** 3 / e2e_s / 1e9
+
+    # ---- roofline of the dominant kernel (FP64 BK axhelm)
+    alg_bytes = 9 * 8 * L  # (2 + 7) words per node: q, Aq, 7 ggeo (axhelm/main.cpp:162)
+    alg_flops = (12 * Nq + 15) * L  # axhelm/main.cpp:165-166
+    peak_bw, peak_src = measured_peaks()
+    achieved = alg_bytes / (ms * 1e-3) / 1e9
+    fp64_peak = nb.peak_fma(True)
+    traffic = load_profile_traffic()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak_bw, "unit": "GB/s",
+                "frac": achieved / peak_bw, "traffic": traffic, "peak_source": peak_src,
+                "binding_roof": {"pipe": "fp64", "achieved_tflops": alg_flops / (ms * 1e-3) / 1e12,
+                                 "issued_tflops": 118 * L / (ms * 1e-3) / 1e12,
+                                 "peak_tflops_measured": fp64_peak,
+                                 "frac": 118 * L / (ms * 1e-3) / 1e12 / fp64_peak}}
+
+    # ---- other precisions of the operator (same mesh, same step definition)
+    variants = {}
+    Df = bp.ptr("Df")
+    q32 = q.float()
+    A32 = torch.empty_like(q32)
+    lam64 = torch.empty(2 * L, dtype=torch.float64, device=dev)
+    nb.fill_uniform(lam64[:L], 1, 1, 0.5, 1.5, stream=stream.cuda_stream)
+    nb.fill_uniform(lam64[L:], 1, 2, 0.5, 2.0, stream=stream.cuda_stream)
+    lam32 = lam64.float()
+    lambf = lam32.to(torch.bfloat16)
+    gf, gb, tri = bp.ptr("ggeo_f"), bp.ptr("ggeo_bf"), bp.ptr("trilinear")
+    torch.cuda.synchronize()
+    for name, flags, prec, gg, DD, la, qq, aa, bpn in [
+            ("fp64_helmholtz", 0, nb.FP64, g, D, lam64, q, Aq, 88),
+            ("fp32_bk", nb.AX_BK, nb.FP32, gf, Df, None, q32, A32, 36),
+            ("fp32_helmholtz", 0, nb.FP32, gf, Df, lam32, q32, A32, 44),
+            ("bf16_helmholtz", 0, nb.BF16, gb, Df, lambf, q32, A32, 26),
+            ("fp32_trilinear_bk", nb.AX_BK, nb.FP32_TRILINEAR, tri, Df, None, q32, A32, 8),
+            ("fp32_trilinear_helmholtz", 0, nb.FP32_TRILINEAR, tri, Df, lam32, q32, A32, 16)]:
+        t = time_axhelm(nb, torch, Nq, flags, prec, E, L, gg, DD, la, qq, aa, 10, 3, stream)
+        variants[name] = {"ms": t, "gdofs": E * N_ORDER ** 3 / (t * 1e-3) / 1e9,
+                          "alg_gbs": bpn * L / (t * 1e-3) / 1e9,
+                          "hbm_frac": bpn * L / (t * 1e-3) / 1e9 / peak_bw}
+    del q32, A32, lam32, lambf, lam64
+    bp.free()
+    del bp
+    torch.cuda.empty_cache()
+
+    pcg = None
+    if not args.no_pcg:
+        pcg = pcg_comparison(nb, torch, dev, args.pcg_n, not args.no_learned)
+
+    cpu = CpuAxhelm().rate(args.cpu_seconds) if (rank == 0 and ws == 1) else None
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": gdofs, "unit": "GDOF/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"axhelm FP64 BK (Poisson) N=7 on E={n}^3={E} perturbed trilinear "
+                               f"box elements per GPU ({L} local nodes, {alg_bytes / 1e9:.1f} GB "
+                               f"per step)", "N": N_ORDER, "E_per_gpu": E,
+                   "l2": "inputs larger than L2 (no flush needed)",
+                   "parallelism": f"replicas x{ws} (element-parallel, no collective)"},
+        "e2e": {"value": e2e_gdofs, "unit": "GDOF/s", "h2d_bytes_per_step": 8 * L,
+                "d2h_bytes_per_step": 8 * L,
+                "note": "nekb_axhelm through the C ABI; q copied from pinned host memory and Aq "
+                        "back every step; geometry resident"},
+        "gpu_launches": args.steps,
+        "roofline": roofline,
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+        "variants": variants,
+        "pcg": pcg,
+        "reference_published": {"v100_axhelm_gdofs": V100_PUBLISHED_GDOFS},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, ws, local = dist_init()
+    if args.impl == "reference":
+        run_reference(args, rank, ws)
+    else:
+        run_gpu(args, rank, ws, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

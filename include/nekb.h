@@ -209,8 +209,10 @@ int nekb_bp_pcg(nekb_bp* bp, const double* lambda, double* r, double* x, double 
  * Per-element 3D convolution network: layers of 3x3x3 convolutions on the Nq^3
  * nodes of each element (zero padding at the element boundary), channels
  * 1 -> C -> ... -> C -> 1, tanh-form GELU between layers, BF16 weights with
- * FP32 accumulation.  Used as z = Jacobi(r) + gs(invDegree * net(r_e/|r_e|)*|r_e|)
- * inside flexible PCG.  No counterpart in the reference (spec extension). */
+ * FP32 accumulation.  Used inside flexible PCG as
+ *   z = invDiag*r + mask(gs(invDegree * s_e * d_e * net(r_e / s_e)))
+ * with s_e the RMS of r over element e and d_e the element's mean invDiag.
+ * No counterpart in the reference. */
 typedef struct nekb_net nekb_net;
 nekb_net* nekb_net_create(int Nq, int channels, int layers, uint64_t seed, int* status);
 void nekb_net_free(nekb_net* net);
@@ -228,9 +230,10 @@ int nekb_net_train_step(nekb_net* net, int64_t E, const float* in, const float* 
 /* gradient of the loss w.r.t. the FP32 master weights (host float array), no update */
 int nekb_net_gradient(nekb_net* net, int64_t E, const float* in, const float* target, float* grad,
                       float* loss, void* stream);
-/* training pairs from solver snapshots: per element e, s_e = RMS(r_e),
- * in_e = r_e / s_e and target_e = (err_e - invDiag*r_e) / s_e (device float
- * arrays of E*Np; invDiag of Efield*Np may be NULL) */
+/* training pairs from solver snapshots: per element e, s_e = RMS(r_e), d_e =
+ * mean of invDiag over the element, in_e = r_e / s_e and target_e =
+ * (err_e - invDiag*r_e) / (s_e d_e) (device float arrays of E*Np; invDiag of
+ * Efield*Np may be NULL, then d_e = 1 and the Jacobi term is dropped) */
 int nekb_net_prepare_pairs(int Np, int64_t E, int64_t Efield, const float* r, const float* err,
                            const float* invDiag, float* in, float* target, void* stream);
 /* versioned checkpoint (header, sizes, step, weights, Adam moments, CRC-32) */

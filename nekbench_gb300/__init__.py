@@ -371,6 +371,74 @@ class BP:
             pass
 
 
+class Net:
+    """Learned element preconditioner (3 layers of 3x3x3 convolutions per element)."""
+
+    def __init__(self, Nq=8, channels=16, layers=3, seed=1, _handle=None):
+        if _handle is not None:
+            self.h = _handle
+        else:
+            st = C.c_int(0)
+            self.h = lib().nekb_net_create(Nq, channels, layers, seed, C.byref(st))
+            check(st.value)
+        self.P = lib().nekb_net_num_params(self.h)
+
+    @classmethod
+    def load(cls, path):
+        st = C.c_int(0)
+        h = lib().nekb_net_load(os.fsencode(path), C.byref(st))
+        check(st.value)
+        return cls(_handle=h)
+
+    def save(self, path):
+        check(lib().nekb_net_save(self.h, os.fsencode(path)))
+
+    def weights(self):
+        import numpy as np
+        w = np.zeros(self.P, dtype=np.float32)
+        check(lib().nekb_net_get_weights(self.h, w.ctypes.data))
+        return w
+
+    def set_weights(self, w):
+        import numpy as np
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        assert w.size == self.P
+        check(lib().nekb_net_set_weights(self.h, w.ctypes.data))
+
+    def forward(self, inp, out, E, stream=None):
+        check(lib().nekb_net_forward(self.h, E, _ptr(inp), _ptr(out), _stream(stream)))
+
+    def gradient(self, inp, target, E, stream=None):
+        import numpy as np
+        g = np.zeros(self.P, dtype=np.float32)
+        loss = C.c_float(0)
+        check(lib().nekb_net_gradient(self.h, E, _ptr(inp), _ptr(target), g.ctypes.data,
+                                      C.byref(loss), _stream(stream)))
+        return g, loss.value
+
+    def train_step(self, inp, target, E, lr, stream=None):
+        loss = C.c_float(0)
+        check(lib().nekb_net_train_step(self.h, E, _ptr(inp), _ptr(target), C.c_float(lr),
+                                        C.byref(loss), _stream(stream)))
+        return loss.value
+
+    def free(self):
+        if getattr(self, "h", None):
+            lib().nekb_net_free(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def prepare_pairs(Np, E, Efield, r, err, inv_diag, inp, target, stream=None):
+    check(lib().nekb_net_prepare_pairs(Np, E, Efield, _ptr(r), _ptr(err), _ptr(inv_diag),
+                                       _ptr(inp), _ptr(target), _stream(stream)))
+
+
 def peak_fma(fp64=True):
     v = C.c_double(0)
     check(lib().nekb_peak_fma(int(fp64), C.byref(v)))

@@ -133,11 +133,15 @@ __device__ void load_weights(const TW* W, float* sW, int C)
   }
 }
 
+// normalize: input r_e / s_e with s_e = RMS(r_e); output times w * s_e * d_e,
+// d_e = mean of invDiag over the element (1 without invDiag), which makes the
+// learned map independent of the mesh size h.
 template <int NQ, int C>
 __global__ void __launch_bounds__(threads_of(NQ))
 k_net_infer(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ Wbf,
-            const float* __restrict__ r, const float* __restrict__ w, float* __restrict__ out,
-            int normalize, const int* skip)
+            const float* __restrict__ r, const float* __restrict__ w,
+            const float* __restrict__ invDiag, float* __restrict__ out, int normalize,
+            const int* skip)
 {
   if (skip != nullptr && *skip != 0) return;
   constexpr int NP = np_of(NQ), P = nparams(C), o2 = kTaps * C, o3 = kTaps * C + kTaps * C * C;
@@ -154,8 +158,9 @@ k_net_infer(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ Wbf,
   const unsigned msk = act ? tap_mask<NQ>(i, j, k) : 0u;
   for (int64_t e = blockIdx.x; e < Etot; e += gridDim.x) {
     const float v = act ? r[e * NP + n] : 0.f;
-    float s = 1.f;
+    float s = 1.f, dmean = 1.f;
     if (normalize) s = sqrtf(block_sum_f(v * v, red) / NP);
+    if (invDiag) dmean = block_sum_f(act ? invDiag[(e % Efield) * NP + n] : 0.f, red) / NP;
     const float inv = s > 0.f ? 1.f / s : 0.f;
     if (act) a0[n] = v * inv;
     __syncthreads();
@@ -177,7 +182,7 @@ k_net_infer(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ Wbf,
       float acc[1];
       conv_fwd<NQ, C, 1>(a2, sW + o3, n, msk, acc);
       const float wn = w ? w[(e % Efield) * NP + n] : 1.f;
-      out[e * NP + n] = wn * s * acc[0];
+      out[e * NP + n] = wn * s * dmean * acc[0];
     }
     __syncthreads();
   }
@@ -365,7 +370,8 @@ __global__ void k_net_combine(int64_t N, int64_t Nloc, const float* __restrict__
     z[n] = zn[n] + invDiag[n % Nloc] * r[n];
 }
 
-// in = r_e / s_e ; target = (e_e - invDiag r_e) / s_e, s_e = RMS of r over element e
+// in = r_e / s_e ; target = (e_e - invDiag r_e) / (s_e d_e), s_e = RMS of r over element e,
+// d_e = mean invDiag over the element (1 without invDiag)
 __global__ void k_prepare_pairs(int Np, int64_t Efield, const float* __restrict__ r,
                                 const float* __restrict__ err, const float* __restrict__ invDiag,
                                 float* __restrict__ in, float* __restrict__ target)
@@ -378,13 +384,17 @@ __global__ void k_prepare_pairs(int Np, int64_t Efield, const float* __restrict_
     ss += v * v;
   }
   const float s = sqrtf(block_sum_f(ss, red) / Np);
+  float ds = 0.f;
+  for (int n = threadIdx.x; n < Np; n += blockDim.x) ds += invDiag ? invDiag[(e % Efield) * Np + n] : 0.f;
+  const float dmean = invDiag ? block_sum_f(ds, red) / Np : 1.f;
   const float inv = s > 0.f ? 1.f / s : 0.f;
+  const float tinv = (s > 0.f && dmean > 0.f) ? 1.f / (s * dmean) : 0.f;
   for (int n = threadIdx.x; n < Np; n += blockDim.x) {
     const int64_t id = e * Np + n;
     const float rv = r[id];
     const float dj = invDiag ? invDiag[(e % Efield) * Np + n] * rv : 0.f;
     in[id] = rv * inv;
-    target[id] = (err[id] - dj) * inv;
+    target[id] = (err[id] - dj) * tinv;
   }
 }
 
@@ -395,7 +405,7 @@ constexpr int train_smem() { return (2 * nparams(C) + np_of(NQ) * (2 + 4 * C)) *
 
 template <int NQ, int C>
 int run_infer(const nekb_net* net, int64_t Etot, int64_t Efield, const float* r, const float* w,
-              float* out, int normalize, const int* skip, cudaStream_t s)
+              const float* invDiag, float* out, int normalize, const int* skip, cudaStream_t s)
 {
   constexpr int SM = infer_smem<NQ, C>();
   static bool attr = false;
@@ -412,7 +422,7 @@ int run_infer(const nekb_net* net, int64_t Etot, int64_t Efield, const float* r,
   if (grid > Etot) grid = Etot;
   if (grid < 1) return NEKB_OK;
   k_net_infer<NQ, C><<<(unsigned)grid, threads_of(NQ), SM, s>>>(
-      Etot, Efield, net->Wbf.as<__nv_bfloat16>(), r, w, out, normalize, skip);
+      Etot, Efield, net->Wbf.as<__nv_bfloat16>(), r, w, invDiag, out, normalize, skip);
   NEKB_CUDA(cudaGetLastError());
   return NEKB_OK;
 }
@@ -452,9 +462,9 @@ int run_train(nekb_net* net, int64_t E, const float* in, const float* target, cu
   return fail(NEKB_ERR_UNSUPPORTED, "net: Nq=%d C=%d not built (Nq 4/6/8, C 4/8/16)", net->Nq, net->C);
 
 int net_infer(const nekb_net* net, int64_t Etot, int64_t Efield, const float* r, const float* w,
-              float* out, int normalize, const int* skip, cudaStream_t s)
+              const float* invDiag, float* out, int normalize, const int* skip, cudaStream_t s)
 {
-  NEKB_NET_DISPATCH(run_infer, net, Etot, Efield, r, w, out, normalize, skip, s)
+  NEKB_NET_DISPATCH(run_infer, net, Etot, Efield, r, w, invDiag, out, normalize, skip, s)
 }
 
 int net_train(nekb_net* net, int64_t E, const float* in, const float* target, cudaStream_t s)
@@ -478,7 +488,7 @@ int net_precondition(nekb_bp* bp, nekb_net* net, const float* r, float* z, const
   const int64_t Nall = bp->Nfields * bp->offset;
   NEKB_TRY(bp->net_tmp.ensure(sizeof(float) * Nall));
   float* tmp = bp->net_tmp.as<float>();
-  NEKB_TRY(net_infer(net, bp->Nfields * bp->E, bp->E, r, w, tmp, 1, skip, s));
+  NEKB_TRY(net_infer(net, bp->Nfields * bp->E, bp->E, r, w, invDiag, tmp, 1, skip, s));
   NEKB_TRY(launch_gs_add(bp->ogs->Nmulti, bp->ogs->d_offsets, bp->ogs->d_ids, bp->Nfields,
                          bp->offset, tmp, NEKB_FLOAT, skip, s));
   const unsigned g = (unsigned)std::min<int64_t>((Nall + 255) / 256, 152 * 16);
@@ -581,7 +591,7 @@ int nekb_net_forward(nekb_net* net, int64_t E, const float* in, float* out, void
 {
   if (!net || (E > 0 && (!in || !out)) || E < 0) return fail(NEKB_ERR_INVALID, "net forward: bad arguments");
   if (E == 0) return NEKB_OK;
-  return net_infer(net, E, E, in, nullptr, out, 0, nullptr, static_cast<cudaStream_t>(stream));
+  return net_infer(net, E, E, in, nullptr, nullptr, out, 0, nullptr, static_cast<cudaStream_t>(stream));
 }
 
 int nekb_net_gradient(nekb_net* net, int64_t E, const float* in, const float* target, float* grad,

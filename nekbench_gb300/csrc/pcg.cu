@@ -684,8 +684,8 @@ int solve_mixed(nekb_bp* bp, const double* lambda, double* r, double* x, double 
                              bp->invdeg_f.as<float>(), bp->invDiag32.as<float>(),
                              bp->p32.as<float>(), bp->z32.as<float>(), bp->Ap32.as<float>(),
                              bp->Ap32.as<float>(), mode, learned || o.flexible != 0, true,
-                             inner_tol, maxit, false, o.check_every, o.use_graph != 0, &ext, &it,
-                             &st, &a0, &a1));
+                             inner_tol, maxit, o.fixed_iterations != 0, o.check_every,
+                             o.use_graph != 0, &ext, &it, &st, &a0, &a1));
     total += it;
     outer++;
     if (st == NEKB_ERR_BREAKDOWN) status = st;
@@ -695,7 +695,8 @@ int solve_mixed(nekb_bp* bp, const double* lambda, double* r, double* x, double 
     k_residual<<<vec_grid(Nall), RT, 0, s>>>(Nall, b, bp->Ax.as<double>(), r);
     NEKB_CUDA(cudaGetLastError());
     NEKB_TRY(wdot<double>(bp, bp->ogs->d_invDegree, r, r, bp->Nfields, &rdotr));
-    if (status == NEKB_ERR_BREAKDOWN || it == 0) break;
+    // fixed iteration count: one inner solve of exactly maxit iterations
+    if (status == NEKB_ERR_BREAKDOWN || it == 0 || o.fixed_iterations) break;
   }
   if (rdotr > TOL && status == NEKB_OK) status = NEKB_ERR_NOT_CONVERGED;
   stats->iterations = total;
