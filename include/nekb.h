@@ -47,6 +47,9 @@ extern "C" {
 #define NEKB_BF16            2  /* ggeo and lambda bf16 storage, q/Aq float, FP32 arithmetic */
 #define NEKB_FP32_TRILINEAR  3  /* geometry from 24 trilinear coefficients per element
                                    (float [E][24]) instead of ggeo; q/Aq/lambda float       */
+#define NEKB_FP64_SPLIT      4  /* FP64 arrays as in NEKB_FP64, arithmetic on the FP32 pipes
+                                   in double-float form (~48 bits; agrees with NEKB_FP64 to
+                                   ~1e-14 relative); |values| < 3.4e38; no Partial forms    */
 
 /* gather-scatter data types and ops (3rdParty/ogs/ogs.hpp:128-140) */
 #define NEKB_DOUBLE 0
@@ -153,6 +156,18 @@ typedef struct {
 } nekb_bp_config;
 
 nekb_bp* nekb_bp_setup(const nekb_bp_config* cfg, void* stream, int* status);
+/* The same state on the caller's own mesh, as the reference's setup() /
+ * solveSetup() build it from mesh_t (nekBone/setup.cpp:36-367): ggeo (FP64,
+ * reference layout, device or host, copied), global ids (host; 0 = not
+ * assembled, ogs.hpp:42-44), the masked (Dirichlet) node list (host, may be
+ * empty) and, optionally, the 8 vertices per element (host, vertex order of
+ * core/meshSetup.cpp:2363-2410) for the trilinear-geometry inner operator
+ * (NULL: NEKB_FP32_TRILINEAR is unavailable on this problem).  D is the GLL
+ * derivative matrix of order N. */
+nekb_bp* nekb_bp_setup_mesh(int N, int64_t Nelements, int Nfields, const double* ggeo,
+                            const int64_t* ids, int64_t Nmasked, const int32_t* maskIds,
+                            const double* EX, const double* EY, const double* EZ, void* stream,
+                            int* status);
 void nekb_bp_free(nekb_bp* bp);
 /* sizes: [0]=Nq [1]=Nelements [2]=Np [3]=offset (Nlocal) [4]=Nmasked [5]=Nfields */
 int nekb_bp_sizes(const nekb_bp* bp, int64_t* sizes6);
@@ -184,22 +199,35 @@ typedef struct {
   int fixed_iterations; /* 1: run exactly maxit iterations                      */
   int bk;               /* 1: Poisson operator (lambda0=1, lambda1=0)           */
   int inner_precision;  /* NEKB_FP32, NEKB_BF16 or NEKB_FP32_TRILINEAR (mixed)  */
-  double inner_tol;     /* relative tolerance of each inner solve (mixed)       */
-  int max_outer;        /* refinement steps (mixed)                             */
+  double inner_tol;     /* mixed: residual reduction between two replacements of
+                           the FP32 residual by the true FP64 one (1e-2)       */
+  int max_outer;        /* mixed: limit on FP64 residual replacements           */
   int check_every;      /* iterations between host convergence checks           */
   int use_graph;        /* 1: replay each chunk of iterations as a CUDA graph   */
   const void* net;      /* nekb_net* for NEKB_PRECOND_LEARNED                   */
 } nekb_pcg_opts;
 
 typedef struct {
-  int iterations;        /* BPPCG's return value (total inner for mixed)         */
-  int outer_iterations;  /* refinement steps (mixed)                             */
+  int iterations;        /* BPPCG's return value (FP32 Krylov iterations, mixed) */
+  int outer_iterations;  /* FP64 true-residual evaluations (mixed; 1 for FP64)   */
   int status;            /* NEKB_OK, NEKB_ERR_BREAKDOWN, NEKB_ERR_NOT_CONVERGED  */
   double rdotr0;         /* weighted |r0|^2                                      */
   double rdotr;          /* weighted |r|^2 of the last check                     */
   double true_rel_res;   /* |b - A x|_w / |b|_w in FP64 after the solve          */
   double elapsed_s;      /* device time of the solve                             */
 } nekb_pcg_stats;
+
+/* BPWeightedInnerProduct(BP, o_w, o_a, o_b) (nekBone/solve.cpp:237-259) with the
+ * weightedMultipleInnerProduct2 kernel (nekBone/kernel/utils.okl:413-458):
+ * *wab = sum over the Nfields fields of w[i] a[i+f*offset] b[i+f*offset]
+ * (w device, Nlocal entries; a, b device, Nfields*offset).  Deterministic
+ * fixed-order reduction on the problem's own scratch; result on the host. */
+int nekb_bp_weighted_inner_product(nekb_bp* bp, const double* w, const double* a, const double* b,
+                                   double* wab);
+/* BPWeightedInnerProduct2 (nekBone/solve.cpp:261-287) with weightedInnerProductUpdate
+ * (nekBone/kernel/utils.okl:687-793): wab2[0] = sum w a b, wab2[1] = sum w a a. */
+int nekb_bp_weighted_inner_product2(nekb_bp* bp, const double* w, const double* a,
+                                    const double* b, double* wab2);
 
 void nekb_pcg_default_opts(nekb_pcg_opts* opts);
 int nekb_bp_pcg(nekb_bp* bp, const double* lambda, double* r, double* x, double tol, int maxit,

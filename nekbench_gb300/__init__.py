@@ -25,7 +25,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libnekb_gb300.so")
 
 AX_BK, AX_N3, AX_PARTIAL = 1, 2, 4
-FP64, FP32, BF16, FP32_TRILINEAR = 0, 1, 2, 3
+FP64, FP32, BF16, FP32_TRILINEAR, FP64_SPLIT = 0, 1, 2, 3, 4
 DOUBLE, FLOAT = 0, 1
 PRECOND_COPY, PRECOND_JACOBI, PRECOND_LEARNED = 0, 1, 2
 SOLVER_FP64, SOLVER_MIXED = 0, 1
@@ -37,8 +37,10 @@ EXPORTED = [
     "nekb_axhelm_flags_from_name", "nekb_update_jacobi", "nekb_geometric_factors",
     "nekb_trilinear_coeffs", "nekb_gll", "nekb_gauss", "nekb_dmatrix", "nekb_fill_uniform",
     "nekb_ogs_setup", "nekb_ogs_free", "nekb_ogs_gs_many", "nekb_ogs_sizes", "nekb_ogs_copy_csr",
-    "nekb_ogs_inv_degree", "nekb_mask", "nekb_bp_setup", "nekb_bp_free", "nekb_bp_sizes",
-    "nekb_bp_device_ptr", "nekb_bp_ogs", "nekb_bp_apply", "nekb_pcg_default_opts", "nekb_bp_pcg",
+    "nekb_ogs_inv_degree", "nekb_mask", "nekb_bp_setup", "nekb_bp_setup_mesh", "nekb_bp_free",
+    "nekb_bp_sizes",
+    "nekb_bp_device_ptr", "nekb_bp_ogs", "nekb_bp_apply", "nekb_bp_weighted_inner_product",
+    "nekb_bp_weighted_inner_product2", "nekb_pcg_default_opts", "nekb_bp_pcg",
     "nekb_net_create", "nekb_net_free", "nekb_net_num_params", "nekb_net_get_weights",
     "nekb_net_set_weights", "nekb_net_forward", "nekb_net_train_step", "nekb_net_gradient",
     "nekb_net_prepare_pairs", "nekb_net_save", "nekb_net_load", "nekb_peak_fma", "nekb_peak_copy",
@@ -107,6 +109,9 @@ def lib():
     L.nekb_mask.argtypes = [i64, vp, vp, i32, vp]
     L.nekb_bp_setup.restype = vp
     L.nekb_bp_setup.argtypes = [C.POINTER(BPConfig), vp, C.POINTER(C.c_int)]
+    L.nekb_bp_setup_mesh.restype = vp
+    L.nekb_bp_setup_mesh.argtypes = [i32, i64, i32, vp, vp, i64, vp, vp, vp, vp, vp,
+                                     C.POINTER(C.c_int)]
     L.nekb_bp_free.argtypes = [vp]
     L.nekb_bp_sizes.argtypes = [vp, vp]
     L.nekb_bp_device_ptr.restype = vp
@@ -114,6 +119,8 @@ def lib():
     L.nekb_bp_ogs.restype = vp
     L.nekb_bp_ogs.argtypes = [vp]
     L.nekb_bp_apply.argtypes = [vp, i32, i32, vp, vp, vp]
+    L.nekb_bp_weighted_inner_product.argtypes = [vp, vp, vp, vp, vp]
+    L.nekb_bp_weighted_inner_product2.argtypes = [vp, vp, vp, vp, vp]
     L.nekb_pcg_default_opts.argtypes = [C.POINTER(PcgOpts)]
     L.nekb_bp_pcg.argtypes = [vp, vp, vp, vp, d, i32, C.POINTER(PcgOpts), C.POINTER(PcgStats)]
     if hasattr(L, "nekb_net_create"):
@@ -323,6 +330,34 @@ class BP:
         self.Nlocal = self.E * self.Np
         self.ogs = OGS(None, _handle=lib().nekb_bp_ogs(self.h), _owner=self)
 
+    @classmethod
+    def from_mesh(cls, N, Nelements, ggeo, ids, mask_ids=None, EX=None, EY=None, EZ=None,
+                  Nfields=1, stream=None):
+        """Problem on the caller's mesh (ggeo device/host FP64 in the reference
+        layout, global ids host int64, masked node list host int32, optional
+        8 vertices per element)."""
+        import numpy as np
+        self = cls.__new__(cls)
+        ids = np.ascontiguousarray(ids, dtype=np.int64)
+        mk = np.ascontiguousarray(mask_ids if mask_ids is not None else np.zeros(0), dtype=np.int32)
+        vx = [None if v is None else np.ascontiguousarray(v, dtype=np.float64) for v in (EX, EY, EZ)]
+        gp = ggeo.data_ptr() if hasattr(ggeo, "data_ptr") else \
+            np.ascontiguousarray(ggeo, dtype=np.float64).ctypes.data
+        self._keep = (ggeo, ids, mk, vx)
+        st = C.c_int(0)
+        self.h = lib().nekb_bp_setup_mesh(
+            N, Nelements, Nfields, gp, ids.ctypes.data, len(mk),
+            mk.ctypes.data if len(mk) else None,
+            *[v.ctypes.data if v is not None else None for v in vx], stream, C.byref(st))
+        check(st.value)
+        s = (C.c_int64 * 6)()
+        check(lib().nekb_bp_sizes(self.h, s))
+        self.Nq, self.E, self.Np, self.offset, self.Nmasked, self.Nfields = list(s)
+        self.N = N
+        self.Nlocal = self.E * self.Np
+        self.ogs = OGS(None, _handle=lib().nekb_bp_ogs(self.h), _owner=self)
+        return self
+
     def device_array(self, name, n, dtype):
         """Copy of a device array owned by the problem, as a torch tensor."""
         import torch
@@ -340,12 +375,25 @@ class BP:
             raise NekbError(ERR_INVALID, lib().nekb_last_error().decode())
         return p
 
+    def weighted_inner_product(self, w, a, b):
+        """BPWeightedInnerProduct: sum over fields of w a b (host float)."""
+        out = C.c_double(0)
+        check(lib().nekb_bp_weighted_inner_product(self.h, _ptr(w), _ptr(a), _ptr(b),
+                                                   C.byref(out)))
+        return out.value
+
+    def weighted_inner_product2(self, w, a, b):
+        """BPWeightedInnerProduct2: (sum w a b, sum w a a)."""
+        out = (C.c_double * 2)()
+        check(lib().nekb_bp_weighted_inner_product2(self.h, _ptr(w), _ptr(a), _ptr(b), out))
+        return out[0], out[1]
+
     def apply(self, q, Aq, lam=None, bk=False, precision=FP64):
         check(lib().nekb_bp_apply(self.h, int(bk), precision, _ptr(lam), _ptr(q), _ptr(Aq)))
 
     def pcg(self, lam, r, x, tol, maxit, solver=SOLVER_FP64, precond=PRECOND_JACOBI,
             flexible=False, fixed_iterations=False, bk=False, inner_precision=FP32_TRILINEAR,
-            inner_tol=1e-3, max_outer=20, check_every=16, use_graph=True, net=None):
+            inner_tol=1e-2, max_outer=40, check_every=16, use_graph=True, net=None):
         """BPPCG: r (rhs in, residual out) and x (guess in, solution out) are device FP64."""
         o = PcgOpts()
         lib().nekb_pcg_default_opts(C.byref(o))

@@ -48,6 +48,8 @@ struct Cfg {
   static constexpr int THREADS = ((NEL * NQ2 + 31) / 32) * 32;
   static constexpr int DPAD = ((NQ * (NQ + 1) + 3) / 4) * 4;  // D, rows padded to NQ+1
   static constexpr bool TRI = (PREC == NEKB_FP32_TRILINEAR);
+  // two CTAs per SM for the 4-byte single-field kernels (caps registers at 128)
+  static constexpr int MINB = (sizeof(T) == 4 && NF == 1 && THREADS <= 256) ? 2 : 1;
   static constexpr int SMEM = (DPAD + NEL * 3 * NF * NP) * (int)sizeof(T) +
                               (TRI ? (NEL * 24 + 2 * NQ) * 4 : 0);
 };
@@ -74,7 +76,7 @@ __device__ __forceinline__ void trilinear_G(const float* c, float r, float s, fl
   const float b0 = -(yr * zt - zr * yt), b1 = xr * zt - zr * xt, b2 = -(xr * yt - yr * xt);
   const float c0 = yr * zs - zr * ys, c1 = -(xr * zs - zr * xs), c2 = xr * ys - yr * xs;
   const float J = xr * a0 + yr * a1 + zr * a2;
-  const float winv = wijk / J;
+  const float winv = __fdividef(wijk, J);  // J > 0 and O(h^3): the fast divide is exact enough
   GwJ = J * wijk;
   G00 = winv * (a0 * a0 + a1 * a1 + a2 * a2);
   G01 = winv * (a0 * b0 + a1 * b1 + a2 * b2);
@@ -85,7 +87,7 @@ __device__ __forceinline__ void trilinear_G(const float* c, float r, float s, fl
 }
 
 template <int NQ, int NF, bool BK, bool PARTIAL, int PREC>
-__global__ void __launch_bounds__(Cfg<NQ, NF, PREC>::THREADS)
+__global__ void __launch_bounds__(Cfg<NQ, NF, PREC>::THREADS, Cfg<NQ, NF, PREC>::MINB)
 k_axhelm(const AxArgs a)
 {
   using C = Cfg<NQ, NF, PREC>;
@@ -134,6 +136,31 @@ k_axhelm(const AxArgs a)
   T* s_Gr = s_q + NF * NP;
   T* s_Gs = s_Gr + NF * NP;
 
+  const TG* ge = static_cast<const TG*>(a.ggeo) + element * 7 * NP + ij;
+  const TG* lam = static_cast<const TG*>(a.lambda);
+  // 4-byte arithmetic with stored geometry is HBM-bound: the whole column's
+  // geometric factors and lambdas are requested before the first barrier so
+  // that every load of the element is in flight at once
+  constexpr bool PF = (sizeof(T) == 4) && !C::TRI;  // stored geometry
+  constexpr bool PFL = (sizeof(T) == 4) && !BK;     // lambda (also with trilinear geometry)
+  constexpr int NPF = PF ? NQ : 1;
+  TG pG[6][NPF];
+  TG pW[PF && !BK ? NQ : 1], pL0[PFL ? NQ : 1], pL1[PFL ? NQ : 1];
+  if ((PF || PFL) && active) {
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      if constexpr (PF) {
+#pragma unroll
+        for (int sl = 0; sl < 6; ++sl) pG[sl][k] = ge[(sl + 1) * NP + k * NQ2];
+      }
+      if constexpr (PF && !BK) pW[k] = ge[k * NQ2];
+      if constexpr (PFL) {
+        pL0[k] = lam[element * NP + k * NQ2 + ij];
+        pL1[k] = lam[element * NP + k * NQ2 + ij + a.offset];
+      }
+    }
+  }
+
   T r_q[NF][NQ];
   if (active) {
     const T* qe = static_cast<const T*>(a.q) + element * NP + ij;
@@ -149,8 +176,7 @@ k_axhelm(const AxArgs a)
   __syncthreads();
 
   T r_Gt[NF][NQ];
-  const TG* ge = static_cast<const TG*>(a.ggeo) + element * 7 * NP + ij;
-  const TG* lam = static_cast<const TG*>(a.lambda);
+  float r_gw[C::TRI && !BK ? NQ : 1];  // GwJ of the column, trilinear geometry only
   if (active) {
     float rr = 0.f, ss = 0.f, wij = 0.f;
     if (C::TRI) {
@@ -167,6 +193,14 @@ k_axhelm(const AxArgs a)
         trilinear_G(s_coef + elc * 24, rr, ss, s_r[k], wij * s_w[k], gw, g00, g01, g02, g11, g12,
                     g22);
         G00 = g00; G01 = g01; G02 = g02; G11 = g11; G12 = g12; G22 = g22;
+        if constexpr (C::TRI && !BK) r_gw[k] = gw;
+      } else if constexpr (PF) {
+        G00 = to_c(pG[0][k]);
+        G01 = to_c(pG[1][k]);
+        G02 = to_c(pG[2][k]);
+        G11 = to_c(pG[3][k]);
+        G12 = to_c(pG[4][k]);
+        G22 = to_c(pG[5][k]);
       } else {
         G00 = to_c(ge[1 * NP + k * NQ2]);
         G01 = to_c(ge[2 * NP + k * NQ2]);
@@ -176,7 +210,11 @@ k_axhelm(const AxArgs a)
         G22 = to_c(ge[6 * NP + k * NQ2]);
       }
       T lam0 = T(1);
-      if (!BK) lam0 = to_c(lam[element * NP + n]);
+      if constexpr (!BK && PFL) {
+        lam0 = to_c(pL0[k]);
+      } else if constexpr (!BK) {
+        lam0 = to_c(lam[element * NP + n]);
+      }
 #pragma unroll
       for (int f = 0; f < NF; ++f) {
         const T* sq = s_q + f * NP + k * NQ2;
@@ -205,27 +243,23 @@ k_axhelm(const AxArgs a)
 
   if (active) {
     T* Aqe = static_cast<T*>(a.Aq) + element * NP + ij;
-    float rr = 0.f, ss = 0.f, wij = 0.f;
-    if (C::TRI && !BK) {
-      rr = s_r[i];
-      ss = s_r[j];
-      wij = s_w[i] * s_w[j];
-    }
 #pragma unroll
     for (int k = 0; k < NQ; ++k) {
       const int n = k * NQ2 + ij;
       T wl1 = T(0);
       if (!BK) {
-        T GwJ;
-        if (C::TRI) {
-          float gw, g00, g01, g02, g11, g12, g22;
-          trilinear_G(s_coef + elc * 24, rr, ss, s_r[k], wij * s_w[k], gw, g00, g01, g02, g11,
-                      g12, g22);
-          GwJ = gw;
+        T GwJ, lam1;
+        if constexpr (C::TRI && !BK) {
+          GwJ = r_gw[k];
+          lam1 = to_c(pL1[k]);
+        } else if constexpr (PF && !BK) {
+          GwJ = to_c(pW[k]);
+          lam1 = to_c(pL1[k]);
         } else {
           GwJ = to_c(ge[k * NQ2]);
+          lam1 = to_c(lam[element * NP + n + a.offset]);
         }
-        wl1 = GwJ * to_c(lam[element * NP + n + a.offset]);
+        wl1 = GwJ * lam1;
       }
 #pragma unroll
       for (int f = 0; f < NF; ++f) {

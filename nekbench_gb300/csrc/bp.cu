@@ -212,7 +212,104 @@ static int bp_build(nekb_bp* bp, const nekb_bp_config& c, cudaStream_t user_stre
   return NEKB_OK;
 }
 
+// problem on the caller's mesh: ggeo (device, reference layout), global ids
+// (host), mask list (host) and, optionally, the element vertices
+static int bp_build_mesh(nekb_bp* bp, int N, int64_t E, int Nfields, const double* ggeo,
+                         const int64_t* ids, int64_t Nmasked, const int32_t* maskIds,
+                         const double* EX, const double* EY, const double* EZ,
+                         cudaStream_t user_stream)
+{
+  bp->cfg = nekb_bp_config{};
+  bp->cfg.N = N;
+  bp->cfg.Nfields = Nfields;
+  bp->N = N;
+  bp->Nq = N + 1;
+  bp->Np = bp->Nq * bp->Nq * bp->Nq;
+  bp->Nfields = Nfields;
+  bp->E = E;
+  bp->Nlocal = E * bp->Np;
+  bp->offset = bp->Nlocal;
+  if (bp->Nlocal > INT32_MAX) return fail(NEKB_ERR_INVALID, "BP: %lld local nodes exceed 32-bit ids", (long long)bp->Nlocal);
+  if (user_stream) {
+    bp->stream = user_stream;
+  } else {
+    NEKB_CUDA(cudaStreamCreateWithFlags(&bp->stream, cudaStreamNonBlocking));
+    bp->own_stream = true;
+  }
+  cudaStream_t s = bp->stream;
+  NEKB_TRY(gll_nodes(N, bp->r1d, bp->w1d));
+  const int Nq = bp->Nq;
+  const int64_t Nl = bp->Nlocal;
+  NEKB_TRY(bp->ggeo.ensure(sizeof(double) * 7 * Nl));
+  NEKB_CUDA(cudaMemcpyAsync(bp->ggeo.p, ggeo, sizeof(double) * 7 * Nl, cudaMemcpyDefault, s));
+  if (EX && EY && EZ) {
+    for (auto pr : {std::make_pair(&bp->EX, EX), std::make_pair(&bp->EY, EY), std::make_pair(&bp->EZ, EZ)}) {
+      NEKB_TRY(pr.first->ensure(sizeof(double) * 8 * E));
+      NEKB_CUDA(cudaMemcpyAsync(pr.first->p, pr.second, sizeof(double) * 8 * E, cudaMemcpyDefault, s));
+    }
+    NEKB_TRY(bp->tri.ensure(sizeof(float) * 24 * E));
+    NEKB_TRY(launch_trilinear_coeffs(E, bp->EX.as<double>(), bp->EY.as<double>(), bp->EZ.as<double>(),
+                                     bp->tri.as<float>(), s));
+  }
+  std::vector<double> hD(Nq * Nq);
+  deriv_matrix(Nq, bp->r1d, hD.data());
+  std::vector<float> hDf(Nq * Nq);
+  for (int t = 0; t < Nq * Nq; ++t) hDf[t] = (float)hD[t];
+  NEKB_TRY(bp->D.ensure(sizeof(double) * Nq * Nq));
+  NEKB_TRY(bp->Df.ensure(sizeof(float) * Nq * Nq));
+  NEKB_CUDA(cudaMemcpyAsync(bp->D.p, hD.data(), sizeof(double) * Nq * Nq, cudaMemcpyHostToDevice, s));
+  NEKB_CUDA(cudaMemcpyAsync(bp->Df.p, hDf.data(), sizeof(float) * Nq * Nq, cudaMemcpyHostToDevice, s));
+  bp->ogs = new nekb_ogs();
+  NEKB_TRY(nekb_ogs_build(bp->ogs, Nl, ids));
+  bp->Nmasked = Nmasked;
+  if (Nmasked > 0) {
+    for (int64_t m = 0; m < Nmasked; ++m)
+      if (maskIds[m] < 0 || maskIds[m] >= Nl) return fail(NEKB_ERR_INVALID, "BP: mask id %d out of range", maskIds[m]);
+    NEKB_TRY(bp->mask.ensure(sizeof(int32_t) * Nmasked));
+    NEKB_CUDA(cudaMemcpyAsync(bp->mask.p, maskIds, sizeof(int32_t) * Nmasked, cudaMemcpyHostToDevice, s));
+  }
+  const size_t vb = sizeof(double) * bp->Nfields * bp->offset;
+  for (DeviceBuf* w : {&bp->p, &bp->z, &bp->Ap, &bp->Ax}) {
+    NEKB_TRY(w->ensure(vb));
+    NEKB_CUDA(cudaMemsetAsync(w->p, 0, vb, s));
+  }
+  NEKB_TRY(bp->invDiag.ensure(sizeof(double) * bp->offset));
+  NEKB_TRY(bp->partials.ensure(sizeof(double) * 4 * 4096));
+  NEKB_TRY(bp->counter.ensure(sizeof(unsigned) * 16));
+  NEKB_CUDA(cudaMemsetAsync(bp->counter.p, 0, sizeof(unsigned) * 16, s));
+  NEKB_TRY(bp->state.ensure(sizeof(PcgState)));
+  NEKB_CUDA(cudaMallocHost(&bp->h_state, sizeof(PcgState)));
+  NEKB_CUDA(cudaStreamSynchronize(s));
+  return NEKB_OK;
+}
+
 }  // namespace nekb
+
+nekb_bp* nekb_bp_create_mesh(int N, int64_t E, int Nfields, const double* ggeo, const int64_t* ids,
+                             int64_t Nmasked, const int32_t* maskIds, const double* EX,
+                             const double* EY, const double* EZ, void* stream, int* status)
+{
+  using namespace nekb;
+  int st = NEKB_OK;
+  nekb_bp* bp = nullptr;
+  if (N < 1 || N + 1 > kMaxNq) {
+    st = fail(NEKB_ERR_UNSUPPORTED, "BP: N=%d outside 1..%d", N, kMaxNq - 1);
+  } else if (E < 1 || !ggeo || !ids || Nmasked < 0 || (Nmasked > 0 && !maskIds)) {
+    st = fail(NEKB_ERR_INVALID, "BP: bad mesh arrays");
+  } else if (Nfields != 1 && Nfields != 3) {
+    st = fail(NEKB_ERR_INVALID, "BP: Nfields=%d (1 or 3)", Nfields);
+  } else {
+    bp = new nekb_bp();
+    st = bp_build_mesh(bp, N, E, Nfields, ggeo, ids, Nmasked, maskIds, EX, EY, EZ,
+                       static_cast<cudaStream_t>(stream));
+    if (st != NEKB_OK) {
+      nekb_bp_destroy(bp);
+      bp = nullptr;
+    }
+  }
+  if (status) *status = st;
+  return bp;
+}
 
 void nekb_ogs_release(nekb_ogs* o)
 {

@@ -9,6 +9,9 @@
 int nekb_ogs_build(nekb_ogs* o, int64_t N, const int64_t* ids);
 void nekb_ogs_release(nekb_ogs* o);
 nekb_bp* nekb_bp_create(const nekb_bp_config* cfg, void* stream, int* status);
+nekb_bp* nekb_bp_create_mesh(int N, int64_t E, int Nfields, const double* ggeo, const int64_t* ids,
+                             int64_t Nmasked, const int32_t* maskIds, const double* EX,
+                             const double* EY, const double* EZ, void* stream, int* status);
 void nekb_bp_destroy(nekb_bp* bp);
 
 namespace nekb {
@@ -19,6 +22,8 @@ int bp_pcg(nekb_bp* bp, const double* lambda, double* r, double* x, double tol, 
            const nekb_pcg_opts* opts, nekb_pcg_stats* stats);
 int peak_fma(int fp64, double* tflops);
 int peak_copy(double* gbs);
+int bp_weighted_inner_product(nekb_bp* bp, const double* w, const double* a, const double* b,
+                              bool two, double* host_out);
 }  // namespace nekb
 
 using namespace nekb;
@@ -246,6 +251,15 @@ nekb_bp* nekb_bp_setup(const nekb_bp_config* cfg, void* stream, int* status)
   return nekb_bp_create(cfg, stream, status);
 }
 
+nekb_bp* nekb_bp_setup_mesh(int N, int64_t Nelements, int Nfields, const double* ggeo,
+                            const int64_t* ids, int64_t Nmasked, const int32_t* maskIds,
+                            const double* EX, const double* EY, const double* EZ, void* stream,
+                            int* status)
+{
+  return nekb_bp_create_mesh(N, Nelements, Nfields, ggeo, ids, Nmasked, maskIds, EX, EY, EZ,
+                             stream, status);
+}
+
 void nekb_bp_free(nekb_bp* bp) { nekb_bp_destroy(bp); }
 
 int nekb_bp_sizes(const nekb_bp* bp, int64_t* s)
@@ -275,6 +289,10 @@ void* nekb_bp_device_ptr(nekb_bp* bp, const char* name)
   if (n == "trilinear") return bp->tri.p;
   if (n == "invDiag") return bp->invDiag.p;
   if (n == "x" || n == "y" || n == "z") {
+    if (bp->EX.p == nullptr) {
+      fail(NEKB_ERR_UNSUPPORTED, "bp device ptr: node coordinates need the element vertices");
+      return nullptr;
+    }
     const int64_t Nl = bp->Nlocal;
     if (bp->xyz.p == nullptr) {
       if (bp->xyz.ensure(sizeof(double) * 3 * Nl) != NEKB_OK) return nullptr;
@@ -298,11 +316,26 @@ int nekb_bp_apply(nekb_bp* bp, int bk, int precision, const void* lambda, const 
 {
   if (!bp || !q || !Aq) return fail(NEKB_ERR_INVALID, "bp apply: NULL argument");
   if (!bk && !lambda) return fail(NEKB_ERR_INVALID, "bp apply: lambda is NULL");
-  if (precision != NEKB_FP64) NEKB_TRY(prepare_inner(bp, precision, 1, nullptr, false));
+  if (precision == NEKB_FP32_TRILINEAR && bp->tri.p == nullptr)
+    return fail(NEKB_ERR_UNSUPPORTED, "bp apply: trilinear geometry needs the element vertices");
+  if (precision != NEKB_FP64 && precision != NEKB_FP64_SPLIT)
+    NEKB_TRY(prepare_inner(bp, precision, 1, nullptr, false));
   OpView op = make_op(bp, bk, precision, lambda);
   NEKB_TRY(apply_op(op, q, Aq, nullptr, bp->stream));
   NEKB_CUDA(cudaStreamSynchronize(bp->stream));
   return NEKB_OK;
+}
+
+int nekb_bp_weighted_inner_product(nekb_bp* bp, const double* w, const double* a, const double* b,
+                                   double* wab)
+{
+  return bp_weighted_inner_product(bp, w, a, b, false, wab);
+}
+
+int nekb_bp_weighted_inner_product2(nekb_bp* bp, const double* w, const double* a,
+                                    const double* b, double* wab2)
+{
+  return bp_weighted_inner_product(bp, w, a, b, true, wab2);
 }
 
 void nekb_pcg_default_opts(nekb_pcg_opts* o)
@@ -312,7 +345,7 @@ void nekb_pcg_default_opts(nekb_pcg_opts* o)
   o->solver = NEKB_SOLVER_FP64;
   o->precond = NEKB_PRECOND_JACOBI;
   o->inner_precision = NEKB_FP32_TRILINEAR;
-  o->inner_tol = 1e-3;
+  o->inner_tol = 1e-2;
   o->max_outer = 20;
   o->check_every = 16;
   o->use_graph = 1;

@@ -102,8 +102,21 @@ __device__ __forceinline__ void conv_fwd(const float* in, const float* w, int n,
       if (!(msk & (1u << t))) continue;
       const float x = src[tap_off<NQ>(t)];
       const float* wt = w + (ci * kTaps + t) * COUT;
+      if constexpr (COUT % 4 == 0) {
+        // the COUT weights of one (ci, tap) are contiguous and 16-byte aligned
+        const float4* w4 = reinterpret_cast<const float4*>(wt);
 #pragma unroll
-      for (int co = 0; co < COUT; ++co) acc[co] += wt[co] * x;
+        for (int q = 0; q < COUT / 4; ++q) {
+          const float4 v = w4[q];
+          acc[4 * q + 0] += v.x * x;
+          acc[4 * q + 1] += v.y * x;
+          acc[4 * q + 2] += v.z * x;
+          acc[4 * q + 3] += v.w * x;
+        }
+      } else {
+#pragma unroll
+        for (int co = 0; co < COUT; ++co) acc[co] += wt[co] * x;
+      }
     }
   }
 }

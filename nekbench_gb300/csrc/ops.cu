@@ -24,6 +24,7 @@ NEKB_DECL_AX(f64)
 NEKB_DECL_AX(f32)
 NEKB_DECL_AX(bf16)
 NEKB_DECL_AX(tri)
+NEKB_DECL_AX(x)
 
 #define NEKB_SWITCH_AX(P)                                          \
   switch (Nq) {                                                    \
@@ -51,6 +52,7 @@ int launch_axhelm(int Nq, int flags, int precision, const AxArgs& a, cudaStream_
     case NEKB_FP32: NEKB_SWITCH_AX(f32)
     case NEKB_BF16: NEKB_SWITCH_AX(bf16)
     case NEKB_FP32_TRILINEAR: NEKB_SWITCH_AX(tri)
+    case NEKB_FP64_SPLIT: NEKB_SWITCH_AX(x)
     default: break;
   }
   return fail(NEKB_ERR_UNSUPPORTED, "axhelm: precision %d not supported", precision);

@@ -22,6 +22,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <functional>
 
 namespace nekb {
 
@@ -147,8 +148,29 @@ __device__ void state_after_rz(PcgState* st, double rz, double rr, double zAp)
   st->beta = beta;
 }
 
+// after the residual was replaced by the true one: new rdotz and beta, same
+// iteration (the search direction p is kept)
+__device__ void state_refresh(PcgState* st, double rz, double rr, double zAp)
+{
+  st->rdotz1 = rz;
+  st->rdotr = rr;
+  double beta;
+  if (st->flexible)
+    beta = -st->alpha * zAp / st->rdotz2;
+  else
+    beta = (st->iter <= 1) ? 0.0 : rz / st->rdotz2;
+  if (!isfinite(beta) || !isfinite(rr)) {
+    st->done = 1;
+    st->result = st->iter - 1;
+    st->status = NEKB_ERR_BREAKDOWN;
+    return;
+  }
+  st->zdotAp = zAp;
+  st->beta = beta;
+}
+
 // [x += alpha p; r -= alpha Ap;] z = M r; sums w r z, w r r (, w z Ap)
-template <typename T, int MODE, bool UPDATE, bool FLEX>
+template <typename T, int MODE, bool UPDATE, bool FLEX, bool REFRESH = false>
 __global__ void __launch_bounds__(RT) k_update_rz(PcgArgs<T> a)
 {
   PcgState* st = a.st;
@@ -184,7 +206,12 @@ __global__ void __launch_bounds__(RT) k_update_rz(PcgArgs<T> a)
     }
   }
   double v[3] = {(double)rz, (double)rr, (double)za};
-  if (grid_sum<3>(v, a.partials, a.counter)) state_after_rz(st, v[0], v[1], v[2]);
+  if (grid_sum<3>(v, a.partials, a.counter)) {
+    if (REFRESH)
+      state_refresh(st, v[0], v[1], v[2]);
+    else
+      state_after_rz(st, v[0], v[1], v[2]);
+  }
 }
 
 // x += alpha p ; r -= alpha Ap (external preconditioner path)
@@ -240,20 +267,59 @@ __global__ void __launch_bounds__(RT) k_pap(PcgArgs<T> a)
   }
 }
 
-// out = sum w a b over fields
-template <typename T>
+}  // namespace
+
+// out[0] = sum w u v over fields (weightedMultipleInnerProduct2, utils.okl:413);
+// with TWO also out[1] = sum w u u (weightedInnerProductUpdate, utils.okl:687)
+template <typename T, bool TWO>
 __global__ void __launch_bounds__(RT) k_wdot(PcgArgs<T> a, const T* u, const T* v2)
 {
-  T acc = 0;
+  T acc = 0, acc2 = 0;
   const int64_t stride = (int64_t)gridDim.x * RT;
   for (int f = 0; f < a.NF; ++f) {
     const int64_t fo = f * a.offset;
-    for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < a.Nloc; i += stride)
-      acc += a.w[i] * u[i + fo] * v2[i + fo];
+    for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < a.Nloc; i += stride) {
+      const T wu = a.w[i] * u[i + fo];
+      acc += wu * v2[i + fo];
+      if (TWO) acc2 += wu * u[i + fo];
+    }
   }
-  double v[1] = {(double)acc};
-  if (grid_sum<1>(v, a.partials, a.counter)) *a.out = v[0];
+  if (TWO) {
+    double v[2] = {(double)acc, (double)acc2};
+    if (grid_sum<2>(v, a.partials, a.counter)) {
+      a.out[0] = v[0];
+      a.out[1] = v[1];
+    }
+  } else {
+    double v[1] = {(double)acc};
+    if (grid_sum<1>(v, a.partials, a.counter)) *a.out = v[0];
+  }
 }
+
+// launch of the weighted inner products on caller-provided scratch: partials
+// (NV doubles per block), a zeroed counter, and out (NV doubles, device)
+int launch_wdot(int64_t N, int NF, int64_t offset, const double* w, const double* u,
+                const double* v, bool two, int64_t grid, double* partials, unsigned* counter,
+                double* out, cudaStream_t s)
+{
+  PcgArgs<double> a{};
+  a.Nloc = N;
+  a.offset = offset;
+  a.NF = NF;
+  a.w = w;
+  a.partials = partials;
+  a.counter = counter;
+  a.out = out;
+  if (grid < 1 || grid > INT32_MAX) return fail(NEKB_ERR_INVALID, "weighted inner product: grid %lld", (long long)grid);
+  if (two)
+    k_wdot<double, true><<<(unsigned)grid, RT, 0, s>>>(a, u, v);
+  else
+    k_wdot<double, false><<<(unsigned)grid, RT, 0, s>>>(a, u, v);
+  NEKB_CUDA(cudaGetLastError());
+  return NEKB_OK;
+}
+
+namespace {
 
 // y = alpha x + beta y
 template <typename T>
@@ -400,19 +466,53 @@ int wdot(nekb_bp* bp, const T* w, const T* u, const T* v, int NF, double* result
   a.partials = bp->partials.as<double>();
   a.counter = bp->counter.as<unsigned>() + 4;
   a.out = bp->partials.as<double>() + 3 * 4096;
-  k_wdot<T><<<red_grid(a.Nloc), RT, 0, bp->stream>>>(a, u, v);
+  k_wdot<T, false><<<red_grid(a.Nloc), RT, 0, bp->stream>>>(a, u, v);
   NEKB_CUDA(cudaGetLastError());
   NEKB_CUDA(cudaMemcpyAsync(result, a.out, sizeof(double), cudaMemcpyDeviceToHost, bp->stream));
   NEKB_CUDA(cudaStreamSynchronize(bp->stream));
   return NEKB_OK;
 }
 
+// z = M r and the (r, z) sums again after the residual was replaced; the
+// iteration count and the search direction stay
+template <typename T>
+int launch_refresh_rz(PcgArgs<T> a, int mode, bool flex, const ExtPrecond* ext, cudaStream_t s)
+{
+  const unsigned rg = red_grid(a.Nloc);
+  if (mode == PC_EXTERNAL) {
+    if constexpr (sizeof(T) == 4) {
+      NEKB_TRY(net_precondition(ext->bp, ext->net, a.r, a.z, ext->invDiag, ext->w, &a.st->done, s));
+    }
+    if (flex)
+      k_update_rz<T, PC_EXTERNAL, false, true, true><<<rg, RT, 0, s>>>(a);
+    else
+      k_update_rz<T, PC_EXTERNAL, false, false, true><<<rg, RT, 0, s>>>(a);
+  } else if (mode == PC_JACOBI) {
+    if (flex)
+      k_update_rz<T, PC_JACOBI, false, true, true><<<rg, RT, 0, s>>>(a);
+    else
+      k_update_rz<T, PC_JACOBI, false, false, true><<<rg, RT, 0, s>>>(a);
+  } else {
+    if (flex)
+      k_update_rz<T, PC_COPY, false, true, true><<<rg, RT, 0, s>>>(a);
+    else
+      k_update_rz<T, PC_COPY, false, false, true><<<rg, RT, 0, s>>>(a);
+  }
+  NEKB_CUDA(cudaGetLastError());
+  return NEKB_OK;
+}
+
+// called after every chunk with the state in bp->h_state; sets *finish to end
+// the iteration (without a hook the iteration ends when the state says done)
+template <typename T>
+using ChunkHook = std::function<int(PcgArgs<T>& a, bool* finish)>;
+
 // PCG on (r, x) with operator op.  Workspace p, z, Ap, Ax of Nfields*offset.
 template <typename T>
 int pcg_core(nekb_bp* bp, const OpView& op, T* r, T* x, const T* w, const T* invDiag, T* p, T* z,
              T* Ap, T* Ax, int mode, bool flex, bool x_is_zero, double tol, int maxit,
              bool fixed, int chunk, bool use_graph, const ExtPrecond* ext, int* iters, int* status,
-             double* rdotr0, double* rdotr)
+             double* rdotr0, double* rdotr, const ChunkHook<T>* hook = nullptr)
 {
   cudaStream_t s = bp->stream;
   const int NF = op.Nfields;
@@ -485,7 +585,8 @@ int pcg_core(nekb_bp* bp, const OpView& op, T* r, T* x, const T* w, const T* inv
     }
   }
 
-  const int max_chunks = (maxit + 1 + chunk - 1) / chunk + 1;
+  // a hook may resume a finished state (residual replacement): allow for that
+  const int max_chunks = (maxit + 1 + chunk - 1) / chunk + 1 + (hook ? 256 : 0);
   for (int c = 0; c < max_chunks; ++c) {
     if (gexec) {
       NEKB_CUDA(cudaGraphLaunch(gexec, s));
@@ -494,9 +595,22 @@ int pcg_core(nekb_bp* bp, const OpView& op, T* r, T* x, const T* w, const T* inv
     }
     NEKB_CUDA(cudaMemcpyAsync(bp->h_state, st, sizeof(PcgState), cudaMemcpyDeviceToHost, s));
     NEKB_CUDA(cudaStreamSynchronize(s));
-    if (bp->h_state->done) break;
+    if (hook) {
+      bool finish = false;
+      NEKB_TRY((*hook)(a, &finish));
+      if (finish) break;
+    } else if (bp->h_state->done) {
+      break;
+    }
   }
   const PcgState& hs = *bp->h_state;
+  if (hook) {  // the hook decided; completed iterations = rz evaluations - 1
+    *iters = hs.iter - 1;
+    *status = hs.status;
+    *rdotr0 = hs.rdotr0;
+    *rdotr = hs.rdotr;
+    return NEKB_OK;
+  }
   if (!hs.done) return fail(NEKB_ERR_CUDA, "PCG: iteration state did not terminate");
   *iters = hs.result;
   *status = hs.status;
@@ -556,6 +670,7 @@ OpView make_op(nekb_bp* bp, int bk, int precision, const void* lambda)
     case NEKB_FP32: op.ggeo = bp->ggeo_f.p; op.D = bp->Df.p; break;
     case NEKB_BF16: op.ggeo = bp->ggeo_bf.p; op.D = bp->Df.p; break;
     case NEKB_FP32_TRILINEAR: op.ggeo = bp->tri.p; op.D = bp->Df.p; break;
+    case NEKB_FP64_SPLIT: op.ggeo = bp->ggeo.p; op.D = bp->D.p; break;
   }
   return op;
 }
@@ -634,8 +749,11 @@ int solve_fp64(nekb_bp* bp, const double* lambda, double* r, double* x, double t
   return NEKB_OK;
 }
 
-// FP64 iterative refinement around an FP32 / BF16 inner PCG:
-//   r = b - A64 x ; while |r|_w > tol |r0|_w : solve A32 d = r/|r| ; x += |r| d
+// Mixed precision: the Krylov iteration runs in FP32 (operator in FP32, BF16
+// storage or FP32 with trilinear geometry) and the solution and true residual
+// are kept in FP64; the FP32 residual is replaced by the FP64 one every time it
+// has dropped by inner_tol (default 1e-2), so the reported residual is always
+// the true FP64 |b - A x|_w and no Krylov information is lost to restarts.
 int solve_mixed(nekb_bp* bp, const double* lambda, double* r, double* x, double tol, int maxit,
                 const nekb_pcg_opts& o, nekb_pcg_stats* stats)
 {
@@ -644,6 +762,8 @@ int solve_mixed(nekb_bp* bp, const double* lambda, double* r, double* x, double 
   const int prec = o.inner_precision;
   if (prec != NEKB_FP32 && prec != NEKB_BF16 && prec != NEKB_FP32_TRILINEAR)
     return fail(NEKB_ERR_INVALID, "mixed solver: inner precision %d", prec);
+  if (prec == NEKB_FP32_TRILINEAR && bp->tri.p == nullptr)
+    return fail(NEKB_ERR_UNSUPPORTED, "mixed solver: trilinear geometry needs the element vertices");
   if (!o.bk && lambda == nullptr) return fail(NEKB_ERR_INVALID, "PCG: lambda is NULL for a Helmholtz solve");
   const bool learned = o.precond == NEKB_PRECOND_LEARNED;
   const bool jacobi = o.precond == NEKB_PRECOND_JACOBI || learned;
@@ -666,37 +786,105 @@ int solve_mixed(nekb_bp* bp, const double* lambda, double* r, double* x, double 
   double rdotr = rdotr0;
   int total = 0, outer = 0, status = NEKB_OK;
   const int max_outer = o.max_outer > 0 ? o.max_outer : 20;
-  const double inner_tol = o.inner_tol > 0 ? o.inner_tol : 1e-3;
+  // residual reduction (in norm) between two replacements of the FP32
+  // recursive residual by the true FP64 one
+  const double delta = o.inner_tol > 0 ? o.inner_tol : 1e-2;
   ExtPrecond ext;
   ext.bp = bp;
   ext.net = (nekb_net*)o.net;
   ext.invDiag = bp->invDiag32.as<float>();
   ext.w = bp->invdeg_f.as<float>();
   const int mode = learned ? PC_EXTERNAL : (jacobi ? PC_JACOBI : PC_COPY);
-  while (rdotr > TOL && outer < max_outer) {
-    const double nr = std::sqrt(rdotr);
-    k_scale_down<<<vec_grid(Nall), RT, 0, s>>>(Nall, 1.0 / nr, r, bp->r32.as<float>());
+  const bool flex = learned || o.flexible != 0;
+  if (rdotr > TOL) {
+    // One FP32 Krylov run on the scaled problem (|r0| = 1).  Whenever its
+    // recursive residual has dropped by delta since the last replacement (or
+    // it believes it converged), the FP32 correction is folded into the FP64
+    // x, the true residual r = b - A64 x is formed in FP64, and it replaces
+    // the FP32 residual; the search direction is kept (reliable updates).
+    const double s0 = 1.0 / std::sqrt(rdotr0);
+    float* r32 = bp->r32.as<float>();
+    float* x32 = bp->x32.as<float>();
+    k_scale_down<<<vec_grid(Nall), RT, 0, s>>>(Nall, s0, r, r32);
     NEKB_CUDA(cudaGetLastError());
-    NEKB_CUDA(cudaMemsetAsync(bp->x32.p, 0, sizeof(float) * Nall, s));
+    NEKB_CUDA(cudaMemsetAsync(x32, 0, sizeof(float) * Nall, s));
+    double rr_last = 1.0;  // scaled |r|^2 at the last replacement
+    const double TOL32 = TOL * s0 * s0;
+    auto fold = [&]() -> int {  // x += x32/s0 ; x32 = 0 ; r = b - A x ; rdotr
+      k_correct<<<vec_grid(Nall), RT, 0, s>>>(Nall, 1.0 / s0, x32, x);
+      NEKB_CUDA(cudaGetLastError());
+      NEKB_CUDA(cudaMemsetAsync(x32, 0, sizeof(float) * Nall, s));
+      NEKB_TRY(apply_op(op64, x, bp->Ax.p, nullptr, s));
+      k_residual<<<vec_grid(Nall), RT, 0, s>>>(Nall, b, bp->Ax.as<double>(), r);
+      NEKB_CUDA(cudaGetLastError());
+      NEKB_TRY(wdot<double>(bp, bp->ogs->d_invDegree, r, r, bp->Nfields, &rdotr));
+      outer++;
+      return NEKB_OK;
+    };
+    // BF16 storage perturbs the operator by ~1e-3: Krylov directions built with
+    // it do not stay conjugate for the true operator, so there each replacement
+    // restarts the iteration (iterative refinement); FP32 operators keep p.
+    const bool restart = (prec == NEKB_BF16);
+    int done_before = 0;  // iterations of finished restarted segments
+    ChunkHook<float> hook = [&](PcgArgs<float>& a, bool* finish) -> int {
+      PcgState& hs = *bp->h_state;
+      if (o.fixed_iterations) {  // exactly maxit iterations, then one fold
+        if (hs.done) {
+          NEKB_TRY(fold());
+          *finish = true;
+        }
+        return NEKB_OK;
+      }
+      const bool stop = hs.done && hs.status != NEKB_OK;  // breakdown or iteration limit
+      if (!(hs.done || hs.rdotr < delta * delta * rr_last)) return NEKB_OK;
+      NEKB_TRY(fold());
+      if (rdotr <= TOL || stop || outer >= max_outer) {
+        if (hs.status == NEKB_ERR_BREAKDOWN) status = NEKB_ERR_BREAKDOWN;
+        *finish = true;
+        return NEKB_OK;
+      }
+      // replace the FP32 residual and resume the same iteration
+      k_scale_down<<<vec_grid(Nall), RT, 0, s>>>(Nall, s0, r, r32);
+      NEKB_CUDA(cudaGetLastError());
+      rr_last = rdotr * s0 * s0;
+      hs.done = 0;
+      hs.status = NEKB_OK;
+      hs.TOL = TOL32;
+      if (restart) {
+        // a fresh iteration: p = 0, rdotz1 = 1, alpha = beta = 0, counter reset
+        // (iterations so far are kept in done_before; the budget shrinks)
+        const int it_seg = hs.iter - 1;
+        done_before += it_seg > 0 ? it_seg : 0;
+        if (done_before >= maxit) {
+          status = NEKB_ERR_NOT_CONVERGED;
+          *finish = true;
+          return NEKB_OK;
+        }
+        hs.iter = 0;
+        hs.maxit = maxit - done_before;
+        hs.rdotz1 = 1.0;
+        hs.rdotz2 = 0.0;
+        hs.alpha = 0.0;
+        hs.beta = 0.0;
+        NEKB_CUDA(cudaMemsetAsync(a.p, 0, sizeof(float) * Nall, s));
+        NEKB_CUDA(cudaMemsetAsync(a.Ap, 0, sizeof(float) * Nall, s));
+        NEKB_CUDA(cudaMemcpyAsync(a.st, &hs, sizeof(PcgState), cudaMemcpyHostToDevice, s));
+        return launch_first_rz<float>(a, mode, flex, &ext, s);
+      }
+      NEKB_CUDA(cudaMemcpyAsync(a.st, &hs, sizeof(PcgState), cudaMemcpyHostToDevice, s));
+      NEKB_TRY(launch_refresh_rz<float>(a, mode, flex, &ext, s));
+      return NEKB_OK;
+    };
     int it = 0, st = 0;
     double a0 = 0, a1 = 0;
-    NEKB_TRY(pcg_core<float>(bp, op32, bp->r32.as<float>(), bp->x32.as<float>(),
-                             bp->invdeg_f.as<float>(), bp->invDiag32.as<float>(),
-                             bp->p32.as<float>(), bp->z32.as<float>(), bp->Ap32.as<float>(),
-                             bp->Ap32.as<float>(), mode, learned || o.flexible != 0, true,
-                             inner_tol, maxit, o.fixed_iterations != 0, o.check_every,
-                             o.use_graph != 0, &ext, &it, &st, &a0, &a1));
-    total += it;
-    outer++;
+    NEKB_TRY(pcg_core<float>(bp, op32, r32, x32, bp->invdeg_f.as<float>(),
+                             bp->invDiag32.as<float>(), bp->p32.as<float>(), bp->z32.as<float>(),
+                             bp->Ap32.as<float>(), bp->Ap32.as<float>(), mode, flex, true,
+                             std::sqrt(TOL32), maxit, o.fixed_iterations != 0, o.check_every,
+                             o.use_graph != 0,
+                             &ext, &it, &st, &a0, &a1, &hook));
+    total = it + done_before;
     if (st == NEKB_ERR_BREAKDOWN) status = st;
-    k_correct<<<vec_grid(Nall), RT, 0, s>>>(Nall, nr, bp->x32.as<float>(), x);
-    NEKB_CUDA(cudaGetLastError());
-    NEKB_TRY(apply_op(op64, x, bp->Ax.p, nullptr, s));
-    k_residual<<<vec_grid(Nall), RT, 0, s>>>(Nall, b, bp->Ax.as<double>(), r);
-    NEKB_CUDA(cudaGetLastError());
-    NEKB_TRY(wdot<double>(bp, bp->ogs->d_invDegree, r, r, bp->Nfields, &rdotr));
-    // fixed iteration count: one inner solve of exactly maxit iterations
-    if (status == NEKB_ERR_BREAKDOWN || it == 0 || o.fixed_iterations) break;
   }
   if (rdotr > TOL && status == NEKB_OK) status = NEKB_ERR_NOT_CONVERGED;
   stats->iterations = total;
@@ -745,6 +933,21 @@ int bp_pcg(nekb_bp* bp, const double* lambda, double* r, double* x, double tol, 
 int bp_wdot(nekb_bp* bp, const double* u, const double* v, double* out)
 {
   return wdot<double>(bp, bp->ogs->d_invDegree, u, v, bp->Nfields, out);
+}
+
+// BPWeightedInnerProduct / BPWeightedInnerProduct2 on the problem's scratch;
+// results returned to the host like the reference's host-side sums
+int bp_weighted_inner_product(nekb_bp* bp, const double* w, const double* a, const double* b,
+                              bool two, double* host_out)
+{
+  if (!bp || !w || !a || !b || !host_out) return fail(NEKB_ERR_INVALID, "weighted inner product: NULL argument");
+  double* out = bp->partials.as<double>() + 3 * 4096;
+  NEKB_TRY(launch_wdot(bp->Nlocal, bp->Nfields, bp->offset, w, a, b, two,
+                       red_grid(bp->Nlocal), bp->partials.as<double>(),
+                       bp->counter.as<unsigned>() + 8, out, bp->stream));
+  NEKB_CUDA(cudaMemcpyAsync(host_out, out, sizeof(double) * (two ? 2 : 1), cudaMemcpyDeviceToHost, bp->stream));
+  NEKB_CUDA(cudaStreamSynchronize(bp->stream));
+  return NEKB_OK;
 }
 
 }  // namespace nekb

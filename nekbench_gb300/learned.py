@@ -4,8 +4,10 @@ Data: (residual, correction) pairs that the plain Jacobi-PCG itself produces.
 For each seeded problem (lambda0 = 1, lambda1 = 1 + 0.5 sin(2 pi k.x) with
 k ~ U{1..4}^3, f ~ U[-1,1] assembled), the FP32 Jacobi-PCG iterate x_k after
 k iterations (k in SNAPSHOTS) gives the residual r_k = b - A x_k (FP64) and
-the correction e_k = x* - x_k to the converged solution.  A random subset of
-elements of each snapshot becomes training pairs through the library's
+the correction the same PCG makes over its next `horizon` iterations,
+x_{k+horizon} - x_k (a local, smoothing map an element network can learn; the
+remaining global error x* - x_k is available with horizon=0).  A random subset
+of elements of each snapshot becomes training pairs through the library's
 nekb_net_prepare_pairs (element RMS normalisation, Jacobi part removed).
 
 Training runs the network's own fused forward/backward kernels and Adam
@@ -22,7 +24,7 @@ import numpy as np
 
 import nekbench_gb300 as nb
 
-SNAPSHOTS = (5, 20, 60, 150)
+SNAPSHOTS = (0, 10, 40, 120)
 
 
 def coefficients(bp, seed, torch):
@@ -43,8 +45,12 @@ def rhs(bp, seed, torch, dev):
     return f
 
 
-def generate_pairs(bp, seeds, torch, dev, frac=0.125, snapshots=SNAPSHOTS, log=None):
-    """Training pairs (inp, target), float32 device tensors of shape [M, Np]."""
+def generate_pairs(bp, seeds, torch, dev, frac=0.125, snapshots=SNAPSHOTS, horizon=16, log=None):
+    """Training pairs (inp, target), float32 device tensors of shape [M, Np].
+
+    The correction paired with the residual r_k is x_{k+horizon} - x_k, what
+    the Jacobi-PCG itself adds to its iterate over the next `horizon`
+    iterations (horizon=0: the remaining error x* - x_k)."""
     E, Np, L = bp.E, bp.Np, bp.Nlocal
     n_sel = max(1, int(frac * E))
     r = torch.empty(L, dtype=torch.float64, device=dev)
@@ -55,15 +61,23 @@ def generate_pairs(bp, seeds, torch, dev, frac=0.125, snapshots=SNAPSHOTS, log=N
     for s in seeds:
         lam = coefficients(bp, s, torch)
         f = rhs(bp, s, torch, dev)
-        r.copy_(f)
-        xs.zero_()
-        bp.pcg(lam, r, xs, 1e-9, 20000, solver=nb.SOLVER_MIXED)  # converged reference
-        inv_diag = bp.device_array("invDiag", L, torch.float64).float().view(E, Np)
+        if horizon <= 0:
+            r.copy_(f)
+            xs.zero_()
+            bp.pcg(lam, r, xs, 1e-9, 20000, solver=nb.SOLVER_MIXED)  # converged reference
+        inv_diag = None
         rng = np.random.default_rng(10_000 + s)
         for k in snapshots:
+            if horizon > 0:
+                r.copy_(f)
+                xs.zero_()
+                bp.pcg(lam, r, xs, 0.0, k + horizon, solver=nb.SOLVER_MIXED,
+                       fixed_iterations=True, max_outer=1)
             r.copy_(f)
             x.zero_()
             bp.pcg(lam, r, x, 0.0, k, solver=nb.SOLVER_MIXED, fixed_iterations=True, max_outer=1)
+            if inv_diag is None:  # the Jacobi diagonal of this seed's lambda
+                inv_diag = bp.device_array("invDiag", L, torch.float64).float().view(E, Np)
             idx = torch.from_numpy(rng.choice(E, n_sel, replace=False).astype(np.int64)).to(dev)
             rk = r.float().view(E, Np).index_select(0, idx).contiguous()
             ek = (xs - x).float().view(E, Np).index_select(0, idx).contiguous()
@@ -116,17 +130,20 @@ def evaluate(bp, net, seeds, torch, dev, tol=1e-8, inner_precision=None):
         lam = coefficients(bp, s, torch)
         f = rhs(bp, s, torch, dev)
         row = {"seed": int(s)}
+        maxit = 20000
         for name, kw in (("jacobi", {}), ("learned", {"precond": nb.PRECOND_LEARNED, "net": net})):
             best = None
             for _ in range(2):
                 r.copy_(f)
                 x.zero_()
-                st = bp.pcg(lam, r, x, tol, 20000, solver=nb.SOLVER_MIXED,
+                st = bp.pcg(lam, r, x, tol, maxit, solver=nb.SOLVER_MIXED,
                             inner_precision=inner_precision, **kw)
                 if best is None or st["elapsed_s"] < best["elapsed_s"]:
                     best = st
             row[name] = {k: best[k] for k in ("iterations", "outer_iterations", "status",
                                                "true_rel_res", "elapsed_s")}
+            # a network that slows convergence is stopped at 3x the Jacobi count
+            maxit = 3 * max(best["iterations"], 1)
         rows.append(row)
     it_j = np.mean([r_["jacobi"]["iterations"] for r_ in rows])
     it_l = np.mean([r_["learned"]["iterations"] for r_ in rows])

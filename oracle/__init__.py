@@ -258,6 +258,34 @@ def gelu_backward(x, gy):
     return gx
 
 
+def net_forward(Nq, W, x, C):
+    """3-layer element network 1 -> C -> C -> 1 with GELU after layers 1 and 2;
+    W = [W1 (C,1,27), W2 (C,C,27), W3 (1,C,27)] flattened."""
+    o2, o3 = 27 * C, 27 * C + 27 * C * C
+    z1 = conv3d_forward(Nq, W[:o2], x, 1, C)
+    a1 = gelu(z1)
+    z2 = conv3d_forward(Nq, W[o2:o3], a1, C, C)
+    a2 = gelu(z2)
+    y = conv3d_forward(Nq, W[o3:], a2, C, 1)
+    return y, (z1, a1, z2, a2)
+
+
+def net_loss_grad(Nq, W, x, t, C):
+    """loss = mean (net(x) - t)^2 and its gradient w.r.t. W, by the chain rule
+    through the oracle's layer backward passes."""
+    o2, o3 = 27 * C, 27 * C + 27 * C * C
+    y, (z1, a1, z2, a2) = net_forward(Nq, W, x, C)
+    d = y.astype(np.float64) - t
+    loss = float(np.mean(d * d))
+    gy = (2 * d / d.size).astype(np.float32)
+    ga2, gW3 = conv3d_backward(Nq, W[o3:], a2, gy, C, 1)
+    gz2 = gelu_backward(z2, ga2)
+    ga1, gW2 = conv3d_backward(Nq, W[o2:o3], a1, gz2, C, C)
+    gz1 = gelu_backward(z1, ga1)
+    _, gW1 = conv3d_backward(Nq, W[:o2], x, gz1, 1, C, want_gin=False)
+    return loss, np.concatenate([gW1, gW2, gW3])
+
+
 # ----------------------------------------------------------------------------- reference shims
 def ref(Nq: int):
     """The reference's own CPU axhelm compiled for this Nq, or None when not built."""

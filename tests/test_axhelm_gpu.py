@@ -34,18 +34,38 @@ def fields(O, L, nf, seed):
     return lam, q
 
 
+@pytest.mark.parametrize("prec", ["FP64", "FP64_SPLIT"])
 @pytest.mark.parametrize("N", list(range(1, 12)))
 @pytest.mark.parametrize("flags", [0, 1, 2, 3])
-def test_fp64_all_orders_variants(nb, O, dev, N, flags):
+def test_fp64_all_orders_variants(nb, O, dev, N, flags, prec):
     m = O.BoxMesh(N, 3, 2, 2, perturb=0.1, seed=N)  # E=12, not a multiple of the CTA's elements
     E, L = m.E, m.Nlocal
     nf = 3 if flags & nb.AX_N3 else 1
     lam, q = fields(O, L, nf, 100 + N)
     ref = O.axhelm(N + 1, E, L, flags, m.ggeo, m.D, lam, q)
     Aq = torch.zeros(nf * L, dtype=torch.float64, device=dev)
-    nb.axhelm(N + 1, flags, nb.FP64, E, L, T(m.ggeo, dev), T(m.D, dev), T(lam, dev), T(q, dev), Aq)
+    nb.axhelm(N + 1, flags, getattr(nb, prec), E, L, T(m.ggeo, dev), T(m.D, dev), T(lam, dev),
+              T(q, dev), Aq)
     torch.cuda.synchronize()
     assert rel(Aq.cpu().numpy(), ref) < 1e-12
+
+
+def test_fp64_split_large_and_scaled_inputs(nb, O, dev):
+    """Double-float arithmetic keeps 1e-12 at a larger size and for inputs scaled
+    over many orders of magnitude (ggeo ~1e-6, q ~1e5)."""
+    N = 7
+    m = O.BoxMesh(N, 6, 5, 4, perturb=0.1, seed=77)
+    E, L = m.E, m.Nlocal
+    lam, q = fields(O, L, 1, 78)
+    for gs, qs in ((1.0, 1.0), (1e-6, 1e5), (1e3, 1e-7)):
+        g, qq = m.ggeo * gs, q * qs
+        for flags in (0, 1):
+            ref = O.axhelm(N + 1, E, L, flags, g, m.D, lam, qq)
+            Aq = torch.zeros(L, dtype=torch.float64, device=dev)
+            nb.axhelm(N + 1, flags, nb.FP64_SPLIT, E, L, T(g, dev), T(m.D, dev), T(lam, dev),
+                      T(qq, dev), Aq)
+            torch.cuda.synchronize()
+            assert rel(Aq.cpu().numpy(), ref) < 1e-12, (gs, qs, flags)
 
 
 @pytest.mark.parametrize("name", ["axhelm_v0", "axhelm_bk_v0", "axhelm_n3_v0", "axhelm_bk_n3_v0"])

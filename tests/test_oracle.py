@@ -195,29 +195,8 @@ def test_pcg_converges_and_jacobi_helps():
     assert abs(it_f - it_j) <= 1 and rel(x2, x1) < 1e-6
 
 
-def _net_forward(Nq, W, x, C):
-    o2, o3 = 27 * C, 27 * C + 27 * C * C
-    z1 = O.conv3d_forward(Nq, W[:o2], x, 1, C)
-    a1 = O.gelu(z1)
-    z2 = O.conv3d_forward(Nq, W[o2:o3], a1, C, C)
-    a2 = O.gelu(z2)
-    y = O.conv3d_forward(Nq, W[o3:], a2, C, 1)
-    return y, (z1, a1, z2, a2)
-
-
-def net_loss_grad(Nq, W, x, t, C):
-    """loss = mean (net(x) - t)^2 and its gradient, composed from the oracle layers."""
-    o2, o3 = 27 * C, 27 * C + 27 * C * C
-    y, (z1, a1, z2, a2) = _net_forward(Nq, W, x, C)
-    d = y.astype(np.float64) - t
-    loss = np.mean(d * d)
-    gy = (2 * d / d.size).astype(np.float32)
-    ga2, gW3 = O.conv3d_backward(Nq, W[o3:], a2, gy, C, 1)
-    gz2 = O.gelu_backward(z2, ga2)
-    ga1, gW2 = O.conv3d_backward(Nq, W[o2:o3], a1, gz2, C, C)
-    gz1 = O.gelu_backward(z1, ga1)
-    _, gW1 = O.conv3d_backward(Nq, W[:o2], x, gz1, 1, C, want_gin=False)
-    return loss, np.concatenate([gW1, gW2, gW3])
+_net_forward = O.net_forward
+net_loss_grad = O.net_loss_grad
 
 
 def test_network_gradient_by_finite_differences():

@@ -130,3 +130,57 @@ def test_mixed_three_fields(nb, O, dev):
     st = bp.pcg(T(lam, dev), r_d, x_d, 1e-10, 1000, solver=nb.SOLVER_MIXED)
     assert st["status"] == 0 and st["true_rel_res"] <= 1e-10
     assert true_rel_res(obp, f, x_d.cpu().numpy()) <= 1.01e-10
+
+
+def test_mixed_keeps_krylov_information(nb, O, dev):
+    """Residual replacement keeps the FP32 iteration count close to the FP64 one
+    (restarted refinement would repeat the early iterations)."""
+    bp, m = pair(nb, O, 7, 5)
+    obp, lam, f = problem(O, m, 1, 17)
+    r, x = T(f, dev), torch.zeros(len(f), dtype=torch.float64, device=dev)
+    st64 = bp.pcg(T(lam, dev), r, x, 1e-8, 3000)
+    r, x = T(f, dev), torch.zeros(len(f), dtype=torch.float64, device=dev)
+    stm = bp.pcg(T(lam, dev), r, x, 1e-8, 3000, solver=nb.SOLVER_MIXED, inner_precision=nb.FP32)
+    assert stm["status"] == 0 and stm["true_rel_res"] <= 1e-8
+    assert stm["iterations"] <= 1.15 * st64["iterations"] + 16, (stm, st64)
+    assert stm["outer_iterations"] >= 2
+
+
+@pytest.mark.parametrize("with_vertices", [True, False])
+def test_problem_on_callers_mesh(nb, O, dev, with_vertices):
+    """BPPCG on a mesh the caller built (here: the oracle's own mesh arrays)."""
+    m = O.BoxMesh(5, 3, 4, 2, perturb=0.1, seed=21)
+    vx = (m.EX, m.EY, m.EZ) if with_vertices else (None, None, None)
+    bp = nb.BP.from_mesh(5, m.E, T(m.ggeo, dev), m.ids, m.maskIds, *vx)
+    obp, lam, f = problem(O, m, 1, 22)
+    r_h, x_h = f.copy(), np.zeros_like(f)
+    it_o = obp.pcg(r_h, x_h, 1e-8, 1000, precond=1)
+    r_d, x_d = T(f, dev), torch.zeros(len(f), dtype=torch.float64, device=dev)
+    st = bp.pcg(T(lam, dev), r_d, x_d, 1e-8, 1000)
+    assert abs(st["iterations"] - it_o) <= 1 and rel(x_d.cpu().numpy(), x_h) < 1e-7
+    r_d, x_d = T(f, dev), torch.zeros(len(f), dtype=torch.float64, device=dev)
+    prec = nb.FP32_TRILINEAR if with_vertices else nb.FP32
+    st = bp.pcg(T(lam, dev), r_d, x_d, 1e-8, 1000, solver=nb.SOLVER_MIXED, inner_precision=prec)
+    assert st["status"] == 0 and true_rel_res(obp, f, x_d.cpu().numpy()) <= 1.01e-8
+    if not with_vertices:
+        with pytest.raises(nb.NekbError):
+            bp.pcg(T(lam, dev), r_d, x_d, 1e-8, 10, solver=nb.SOLVER_MIXED,
+                   inner_precision=nb.FP32_TRILINEAR)
+
+
+def test_weighted_inner_products(nb, O, dev):
+    """BPWeightedInnerProduct(2) against the oracle's sums (tolerance: different order)."""
+    bp, m = pair(nb, O, 7, 3, Nfields=3)
+    L = bp.Nlocal
+    w = bp.ogs.inv_degree()
+    a = torch.from_numpy(O.uniform(3 * L, 21, 1, -1, 1)).to(dev)
+    b = torch.from_numpy(O.uniform(3 * L, 21, 2, -1, 1)).to(dev)
+    wn, an, bn = w.cpu().numpy(), a.cpu().numpy(), b.cpu().numpy()
+    ref_ab = sum(float(np.sum(wn * an[f * L:(f + 1) * L] * bn[f * L:(f + 1) * L])) for f in range(3))
+    ref_aa = sum(float(np.sum(wn * an[f * L:(f + 1) * L] ** 2)) for f in range(3))
+    got = bp.weighted_inner_product(w, a, b)
+    assert abs(got - ref_ab) <= 1e-12 * abs(ref_ab)
+    g1, g2 = bp.weighted_inner_product2(w, a, b)
+    assert abs(g1 - ref_ab) <= 1e-12 * abs(ref_ab) and abs(g2 - ref_aa) <= 1e-12 * ref_aa
+    # deterministic: repeated calls give identical bits
+    assert bp.weighted_inner_product(w, a, b) == got
