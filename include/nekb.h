@@ -229,6 +229,22 @@ int nekb_bp_weighted_inner_product(nekb_bp* bp, const double* w, const double* a
 int nekb_bp_weighted_inner_product2(nekb_bp* bp, const double* w, const double* a,
                                     const double* b, double* wab2);
 
+/* The same weighted inner product for callers that cannot allocate device
+ * memory: an application whose GPU memory all belongs to its own pool
+ * allocator, or a loop that must not trigger the implicit synchronisation a
+ * cudaMalloc can cause.  No counterpart in the reference.
+ * *wab (a device double) = sum over the Nfields fields of w[i] a[i+f*offset]
+ * b[i+f*offset], i < N, computed on the given stream; nothing is allocated.
+ * The scratch (one partial sum per 256-node block and a completion ticket) is
+ * a fixed 1 MiB array inside the library, held by every GPU that loads the
+ * library until the process exits; N above 33,554,432 nodes per field is
+ * refused with NEKB_ERR_INVALID.  Every call shares that array, so calls that
+ * overlap on the same GPU race.  The first call on a device looks up the
+ * array's device address; make it before any stream capture. */
+int nekb_weighted_inner_product_noalloc(int64_t N, int Nfields, int64_t offset, const double* w,
+                                        const double* a, const double* b, double* wab,
+                                        void* stream);
+
 void nekb_pcg_default_opts(nekb_pcg_opts* opts);
 int nekb_bp_pcg(nekb_bp* bp, const double* lambda, double* r, double* x, double tol, int maxit,
                 const nekb_pcg_opts* opts, nekb_pcg_stats* stats);

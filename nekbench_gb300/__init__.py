@@ -40,7 +40,8 @@ EXPORTED = [
     "nekb_ogs_inv_degree", "nekb_mask", "nekb_bp_setup", "nekb_bp_setup_mesh", "nekb_bp_free",
     "nekb_bp_sizes",
     "nekb_bp_device_ptr", "nekb_bp_ogs", "nekb_bp_apply", "nekb_bp_weighted_inner_product",
-    "nekb_bp_weighted_inner_product2", "nekb_pcg_default_opts", "nekb_bp_pcg",
+    "nekb_bp_weighted_inner_product2", "nekb_weighted_inner_product_noalloc",
+    "nekb_pcg_default_opts", "nekb_bp_pcg",
     "nekb_net_create", "nekb_net_free", "nekb_net_num_params", "nekb_net_get_weights",
     "nekb_net_set_weights", "nekb_net_forward", "nekb_net_train_step", "nekb_net_gradient",
     "nekb_net_prepare_pairs", "nekb_net_save", "nekb_net_load", "nekb_peak_fma", "nekb_peak_copy",
