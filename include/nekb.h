@@ -138,9 +138,11 @@ const double* nekb_ogs_inv_degree(const nekb_ogs* ogs);
 int nekb_mask(int64_t Nmasked, const int32_t* maskIds, void* q, int dtype, void* stream);
 
 /* ------------------------------------------------------------------ benchmark problem
- * Box mesh of nx*ny*nz hexahedra of order N on the unit cube, interior vertices
- * perturbed by U[-perturb*h, perturb*h] (seeded), homogeneous Dirichlet on the
- * boundary (dirichlet=1) or periodic (periodic=1).  Builds on the device the
+ * Box mesh of nx*ny*nz hexahedra of order N on [box_min, box_max]^3 (the unit
+ * cube when box_max <= box_min; the reference's default box is [-1,1]^3,
+ * core/meshSetup.cpp:2316), interior vertices perturbed by
+ * U[-perturb*h, perturb*h] (seeded), homogeneous Dirichlet on the boundary
+ * (dirichlet=1) or periodic (periodic=1).  Builds on the device the
  * geometric factors, gather-scatter handle, mask list and solver workspace:
  * the state the reference keeps in mesh_t and BP_t (nekBone/BP.hpp:47-153,
  * nekBone/setup.cpp:36-367). */
@@ -153,6 +155,7 @@ typedef struct {
   int dirichlet;      /* 1: boundary nodes masked (ids 0)                   */
   double perturb;     /* vertex perturbation fraction of h (0.1 typical)    */
   uint64_t seed;
+  double box_min, box_max; /* extent per direction; box_max <= box_min: [0,1] */
 } nekb_bp_config;
 
 nekb_bp* nekb_bp_setup(const nekb_bp_config* cfg, void* stream, int* status);
@@ -178,6 +181,13 @@ nekb_ogs* nekb_bp_ogs(nekb_bp* bp);
 
 /* full operator used by the solvers: Aq = mask(gs(axhelm(q))) */
 int nekb_bp_apply(nekb_bp* bp, int bk, int precision, const void* lambda, const void* q, void* Aq);
+
+/* BPZeroMean(BP, o_q) (nekBone/solve.cpp:115-134): subtract from every entry
+ * of q (device FP64, Nfields*offset) the mean of its Nelements*Np local values
+ * over all fields (sum kernel utils.okl:212, addScalar utils.okl:29).
+ * Deterministic fixed-order sum; runs on the problem's stream and returns
+ * when it is done. */
+int nekb_bp_zero_mean(nekb_bp* bp, double* q);
 
 /* ------------------------------------------------------------------ PCG
  * BPPCG(BP, o_lambda, o_r, o_x, tol, MAXIT, opElapsed) (nekBone/solve.cpp:44-113,
@@ -205,6 +215,9 @@ typedef struct {
   int check_every;      /* iterations between host convergence checks           */
   int use_graph;        /* 1: replay each chunk of iterations as a CUDA graph   */
   const void* net;      /* nekb_net* for NEKB_PRECOND_LEARNED                   */
+  int zero_mean;        /* 1: nekb_bp_zero_mean on r before and on x after the
+                           solve, as solve() does for an all-Neumann problem
+                           (nekBone/main.cpp:24-31)                             */
 } nekb_pcg_opts;
 
 typedef struct {
@@ -254,11 +267,20 @@ int nekb_bp_pcg(nekb_bp* bp, const double* lambda, double* r, double* x, double 
  * nodes of each element (zero padding at the element boundary), channels
  * 1 -> C -> ... -> C -> 1, tanh-form GELU between layers, BF16 weights with
  * FP32 accumulation.  Used inside flexible PCG as
- *   z = invDiag*r + mask(gs(invDegree * s_e * d_e * net(r_e / s_e)))
- * with s_e the RMS of r over element e and d_e the element's mean invDiag.
+ *   z = invDiag*r + mask(gs(invDegree * h * s_e * net(h * r_e / s_e)))
+ * with h = sqrt(invDiag) per node and s_e the RMS of h*r over element e.
  * No counterpart in the reference. */
 typedef struct nekb_net nekb_net;
 nekb_net* nekb_net_create(int Nq, int channels, int layers, uint64_t seed, int* status);
+/* inference arithmetic: NEKB_NET_TENSOR (default; BF16 tensor-core MMA with
+ * BF16 activations between layers, FP32 sums; built for Nq=8 with 16
+ * channels, other shapes fall back to NEKB_NET_FP32) or NEKB_NET_FP32 (FP32
+ * activations and sums on the CUDA cores).  nekb_net_inference returns the
+ * arithmetic actually used. */
+#define NEKB_NET_FP32   0
+#define NEKB_NET_TENSOR 1
+int nekb_net_set_inference(nekb_net* net, int mode);
+int nekb_net_inference(const nekb_net* net);
 void nekb_net_free(nekb_net* net);
 int nekb_net_num_params(const nekb_net* net);
 /* FP32 master weights (host arrays of nekb_net_num_params floats) */
@@ -274,12 +296,24 @@ int nekb_net_train_step(nekb_net* net, int64_t E, const float* in, const float* 
 /* gradient of the loss w.r.t. the FP32 master weights (host float array), no update */
 int nekb_net_gradient(nekb_net* net, int64_t E, const float* in, const float* target, float* grad,
                       float* loss, void* stream);
-/* training pairs from solver snapshots: per element e, s_e = RMS(r_e), d_e =
- * mean of invDiag over the element, in_e = r_e / s_e and target_e =
- * (err_e - invDiag*r_e) / (s_e d_e) (device float arrays of E*Np; invDiag of
- * Efield*Np may be NULL, then d_e = 1 and the Jacobi term is dropped) */
+/* training pairs from solver snapshots: per element e, h = sqrt(invDiag) per
+ * node, s_e = RMS of h*r_e, in_e = h*r_e / s_e and target_e =
+ * (err_e - invDiag*r_e) / (h s_e) (device float arrays of E*Np; invDiag of
+ * Efield*Np may be NULL, then h = 1 and the Jacobi term is dropped) */
 int nekb_net_prepare_pairs(int Np, int64_t E, int64_t Efield, const float* r, const float* err,
                            const float* invDiag, float* in, float* target, void* stream);
+/* Element-local correction y of n residual rows r (device FP32, [n][Np], row b
+ * taken from element elems[b] of field 0): on the element-interior nodes the
+ * solution of the element's Helmholtz problem A_II y_I = r_I with y = 0 on the
+ * element boundary (FP32 CG, at most iters steps, relative tolerance tol); on
+ * the element-boundary nodes invDiag*r (invDiag rows [n][Np]).  lambda as in
+ * nekb_bp_pcg (2*offset FP64).  Training target for the learned
+ * preconditioner (with nekb_net_prepare_pairs, err = y); an element index
+ * outside the mesh gives a zero row.  Runs on the problem's stream and returns
+ * when it is done.  Nq 3..8.
+ * No counterpart in the reference. */
+int nekb_bp_local_correction(nekb_bp* bp, const double* lambda, const int32_t* elems, int64_t n,
+                             const float* r, const float* invDiag, float* y, int iters, float tol);
 /* versioned checkpoint (header, sizes, step, weights, Adam moments, CRC-32) */
 int nekb_net_save(const nekb_net* net, const char* path);
 nekb_net* nekb_net_load(const char* path, int* status);

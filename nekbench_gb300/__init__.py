@@ -29,6 +29,7 @@ FP64, FP32, BF16, FP32_TRILINEAR, FP64_SPLIT = 0, 1, 2, 3, 4
 DOUBLE, FLOAT = 0, 1
 PRECOND_COPY, PRECOND_JACOBI, PRECOND_LEARNED = 0, 1, 2
 SOLVER_FP64, SOLVER_MIXED = 0, 1
+NET_FP32, NET_TENSOR = 0, 1
 OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_UNSUPPORTED, ERR_BREAKDOWN, ERR_NOT_CONVERGED = \
     0, -1, -2, -3, -4, -5, -6
 
@@ -41,8 +42,9 @@ EXPORTED = [
     "nekb_bp_sizes",
     "nekb_bp_device_ptr", "nekb_bp_ogs", "nekb_bp_apply", "nekb_bp_weighted_inner_product",
     "nekb_bp_weighted_inner_product2", "nekb_weighted_inner_product_noalloc",
-    "nekb_pcg_default_opts", "nekb_bp_pcg",
-    "nekb_net_create", "nekb_net_free", "nekb_net_num_params", "nekb_net_get_weights",
+    "nekb_pcg_default_opts", "nekb_bp_pcg", "nekb_bp_zero_mean", "nekb_bp_local_correction",
+    "nekb_net_create", "nekb_net_free", "nekb_net_set_inference", "nekb_net_inference",
+    "nekb_net_num_params", "nekb_net_get_weights",
     "nekb_net_set_weights", "nekb_net_forward", "nekb_net_train_step", "nekb_net_gradient",
     "nekb_net_prepare_pairs", "nekb_net_save", "nekb_net_load", "nekb_peak_fma", "nekb_peak_copy",
 ]
@@ -57,14 +59,15 @@ class NekbError(RuntimeError):
 class BPConfig(C.Structure):
     _fields_ = [("N", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
                 ("Nfields", C.c_int), ("periodic", C.c_int), ("dirichlet", C.c_int),
-                ("perturb", C.c_double), ("seed", C.c_uint64)]
+                ("perturb", C.c_double), ("seed", C.c_uint64), ("box_min", C.c_double),
+                ("box_max", C.c_double)]
 
 
 class PcgOpts(C.Structure):
     _fields_ = [("solver", C.c_int), ("precond", C.c_int), ("flexible", C.c_int),
                 ("fixed_iterations", C.c_int), ("bk", C.c_int), ("inner_precision", C.c_int),
                 ("inner_tol", C.c_double), ("max_outer", C.c_int), ("check_every", C.c_int),
-                ("use_graph", C.c_int), ("net", C.c_void_p)]
+                ("use_graph", C.c_int), ("net", C.c_void_p), ("zero_mean", C.c_int)]
 
 
 class PcgStats(C.Structure):
@@ -124,10 +127,13 @@ def lib():
     L.nekb_bp_weighted_inner_product2.argtypes = [vp, vp, vp, vp, vp]
     L.nekb_pcg_default_opts.argtypes = [C.POINTER(PcgOpts)]
     L.nekb_bp_pcg.argtypes = [vp, vp, vp, vp, d, i32, C.POINTER(PcgOpts), C.POINTER(PcgStats)]
+    L.nekb_bp_zero_mean.argtypes = [vp, vp]
     if hasattr(L, "nekb_net_create"):
         L.nekb_net_create.restype = vp
         L.nekb_net_create.argtypes = [i32, i32, i32, C.c_uint64, C.POINTER(C.c_int)]
         L.nekb_net_free.argtypes = [vp]
+        L.nekb_net_set_inference.argtypes = [vp, i32]
+        L.nekb_net_inference.argtypes = [vp]
         L.nekb_net_num_params.argtypes = [vp]
         L.nekb_net_get_weights.argtypes = [vp, vp]
         L.nekb_net_set_weights.argtypes = [vp, vp]
@@ -135,6 +141,7 @@ def lib():
         L.nekb_net_train_step.argtypes = [vp, i64, vp, vp, C.c_float, vp, vp]
         L.nekb_net_gradient.argtypes = [vp, i64, vp, vp, vp, vp, vp]
         L.nekb_net_prepare_pairs.argtypes = [i32, i64, i64, vp, vp, vp, vp, vp, vp]
+        L.nekb_bp_local_correction.argtypes = [vp, vp, vp, i64, vp, vp, vp, i32, C.c_float]
         L.nekb_net_save.argtypes = [vp, C.c_char_p]
         L.nekb_net_load.restype = vp
         L.nekb_net_load.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
@@ -150,6 +157,13 @@ def check(code):
     return code
 
 
+def check_value(v):
+    """A non-negative return value, or the error it encodes."""
+    if v < 0:
+        raise NekbError(v, lib().nekb_last_error().decode())
+    return v
+
+
 def _ptr(t):
     if t is None:
         return None
@@ -163,6 +177,14 @@ def _stream(stream):
         import torch
         return torch.cuda.current_stream().cuda_stream
     return stream
+
+
+def _order_after_torch():
+    """The problem's entry points run on its own stream: wait for the work that
+    torch has queued on its current stream (the producers of their inputs)."""
+    import torch
+    if torch.cuda.is_available() and torch.cuda.is_initialized():
+        torch.cuda.current_stream().synchronize()
 
 
 def _require_cuda(*ts):
@@ -317,10 +339,12 @@ class BP:
     """Box-mesh benchmark problem on the device (mesh_t + BP_t of nekBone)."""
 
     def __init__(self, N, nx, ny=None, nz=None, Nfields=1, periodic=False, dirichlet=True,
-                 perturb=0.1, seed=1, stream=None):
+                 perturb=0.1, seed=1, stream=None, box=(0.0, 0.0)):
+        """box=(lo, hi): the cube [lo, hi]^3; (0, 0) is the unit cube."""
         ny = nx if ny is None else ny
         nz = nx if nz is None else nz
-        self.cfg = BPConfig(N, nx, ny, nz, Nfields, int(periodic), int(dirichlet), perturb, seed)
+        self.cfg = BPConfig(N, nx, ny, nz, Nfields, int(periodic), int(dirichlet), perturb, seed,
+                            float(box[0]), float(box[1]))
         st = C.c_int(0)
         self.h = lib().nekb_bp_setup(C.byref(self.cfg), stream, C.byref(st))
         check(st.value)
@@ -379,6 +403,7 @@ class BP:
     def weighted_inner_product(self, w, a, b):
         """BPWeightedInnerProduct: sum over fields of w a b (host float)."""
         out = C.c_double(0)
+        _order_after_torch()
         check(lib().nekb_bp_weighted_inner_product(self.h, _ptr(w), _ptr(a), _ptr(b),
                                                    C.byref(out)))
         return out.value
@@ -386,16 +411,35 @@ class BP:
     def weighted_inner_product2(self, w, a, b):
         """BPWeightedInnerProduct2: (sum w a b, sum w a a)."""
         out = (C.c_double * 2)()
+        _order_after_torch()
         check(lib().nekb_bp_weighted_inner_product2(self.h, _ptr(w), _ptr(a), _ptr(b), out))
         return out[0], out[1]
 
+    def zero_mean(self, q):
+        """BPZeroMean: subtract the mean of the local values over all fields."""
+        _order_after_torch()
+        check(lib().nekb_bp_zero_mean(self.h, _ptr(q)))
+
     def apply(self, q, Aq, lam=None, bk=False, precision=FP64):
+        _order_after_torch()
         check(lib().nekb_bp_apply(self.h, int(bk), precision, _ptr(lam), _ptr(q), _ptr(Aq)))
+
+    def local_correction(self, lam, elems, r, inv_diag, y, iters=200, tol=1e-5):
+        """Element-interior Helmholtz solve of residual rows r [n, Np] (float32,
+        row b from element elems[b], int32) with the Jacobi value invDiag*r on
+        the element-boundary nodes; result in y."""
+        n = int(elems.numel())
+        _order_after_torch()
+        check(lib().nekb_bp_local_correction(self.h, _ptr(lam), _ptr(elems), n, _ptr(r),
+                                             _ptr(inv_diag), _ptr(y), int(iters), float(tol)))
 
     def pcg(self, lam, r, x, tol, maxit, solver=SOLVER_FP64, precond=PRECOND_JACOBI,
             flexible=False, fixed_iterations=False, bk=False, inner_precision=FP32_TRILINEAR,
-            inner_tol=1e-2, max_outer=40, check_every=16, use_graph=True, net=None):
-        """BPPCG: r (rhs in, residual out) and x (guess in, solution out) are device FP64."""
+            inner_tol=1e-2, max_outer=40, check_every=16, use_graph=True, net=None,
+            zero_mean=False):
+        """BPPCG: r (rhs in, residual out) and x (guess in, solution out) are device FP64;
+        zero_mean: BPZeroMean on r before and on x after, as solve() does for an
+        all-Neumann problem."""
         o = PcgOpts()
         lib().nekb_pcg_default_opts(C.byref(o))
         o.solver, o.precond, o.flexible, o.fixed_iterations, o.bk = \
@@ -403,7 +447,9 @@ class BP:
         o.inner_precision, o.inner_tol, o.max_outer = inner_precision, inner_tol, max_outer
         o.check_every, o.use_graph = check_every, int(use_graph)
         o.net = net.h if net is not None else None
+        o.zero_mean = int(zero_mean)
         st = PcgStats()
+        _order_after_torch()
         check(lib().nekb_bp_pcg(self.h, _ptr(lam), _ptr(r), _ptr(x), tol, maxit, C.byref(o),
                                 C.byref(st)))
         return st.as_dict()
@@ -453,6 +499,15 @@ class Net:
         w = np.ascontiguousarray(w, dtype=np.float32)
         assert w.size == self.P
         check(lib().nekb_net_set_weights(self.h, w.ctypes.data))
+
+    @property
+    def inference(self):
+        """NET_TENSOR (BF16 tensor-core MMA) or NET_FP32 (CUDA cores), as used."""
+        return check_value(lib().nekb_net_inference(self.h))
+
+    @inference.setter
+    def inference(self, mode):
+        check(lib().nekb_net_set_inference(self.h, int(mode)))
 
     def forward(self, inp, out, E, stream=None):
         check(lib().nekb_net_forward(self.h, E, _ptr(inp), _ptr(out), _stream(stream)))

@@ -158,6 +158,17 @@ k_axhelm_x(const AxArgs a)
   df* s_Gr = s_q + NF * NP;
   df* s_Gs = s_Gr + NF * NP;
 
+  // geometry of layer k+1 is requested while layer k is computed; layer 0
+  // before the first barrier (the kernel is otherwise waiting on these loads)
+  const double* ge = static_cast<const double*>(a.ggeo) + element * 7 * NP + ij;
+  const double* lam = static_cast<const double*>(a.lambda);
+  double gnext[7];
+  if (active) {
+#pragma unroll
+    for (int sl = 0; sl < 6; ++sl) gnext[sl] = ge[(sl + 1) * NP];
+    if (!BK) gnext[6] = lam[element * NP + ij];
+  }
+
   df r_q[NF][NQ];
   if (active) {
     const double* qe = static_cast<const double*>(a.q) + element * NP + ij;
@@ -173,20 +184,29 @@ k_axhelm_x(const AxArgs a)
   __syncthreads();
 
   df r_Gt[NF][NQ];
-  const double* ge = static_cast<const double*>(a.ggeo) + element * 7 * NP + ij;
-  const double* lam = static_cast<const double*>(a.lambda);
   if (active) {
 #pragma unroll
     for (int k = 0; k < NQ; ++k) {
       const int n = k * NQ2 + ij;
-      const df G00 = split(ge[1 * NP + k * NQ2]);
-      const df G01 = split(ge[2 * NP + k * NQ2]);
-      const df G02 = split(ge[3 * NP + k * NQ2]);
-      const df G11 = split(ge[4 * NP + k * NQ2]);
-      const df G12 = split(ge[5 * NP + k * NQ2]);
-      const df G22 = split(ge[6 * NP + k * NQ2]);
+      double gcur[7];
+#pragma unroll
+      for (int sl = 0; sl < 7; ++sl) gcur[sl] = gnext[sl];
+      if (k + 1 < NQ) {
+#pragma unroll
+        for (int sl = 0; sl < 6; ++sl) gnext[sl] = ge[(sl + 1) * NP + (k + 1) * NQ2];
+        if (!BK) gnext[6] = lam[element * NP + n + NQ2];
+      } else if (!BK) {  // phase 3 starts with layer 0's GwJ and lambda1
+        gnext[0] = ge[0];
+        gnext[1] = lam[element * NP + ij + a.offset];
+      }
+      const df G00 = split(gcur[0]);
+      const df G01 = split(gcur[1]);
+      const df G02 = split(gcur[2]);
+      const df G11 = split(gcur[3]);
+      const df G12 = split(gcur[4]);
+      const df G22 = split(gcur[5]);
       df lam0;
-      if (!BK) lam0 = split(lam[element * NP + n]);
+      if (!BK) lam0 = split(gcur[6]);
 #pragma unroll
       for (int f = 0; f < NF; ++f) {
         const df* sq = s_q + f * NP + k * NQ2;
@@ -223,8 +243,13 @@ k_axhelm_x(const AxArgs a)
       const int n = k * NQ2 + ij;
       df wl1;
       if (!BK) {
+        const double gw = gnext[0], l1 = gnext[1];
+        if (k + 1 < NQ) {
+          gnext[0] = ge[(k + 1) * NQ2];
+          gnext[1] = lam[element * NP + n + NQ2 + a.offset];
+        }
         acc2 t;
-        t.fma2(split(ge[k * NQ2]), split(lam[element * NP + n + a.offset]));
+        t.fma2(split(gw), split(l1));
         wl1 = t.get();
       }
 #pragma unroll

@@ -63,7 +63,9 @@ int apply_op(const OpView& op, const void* q, void* Aq, const int* skip, cudaStr
 static void box_vertices(const nekb_bp_config& c, double* EX, double* EY, double* EZ)
 {
   const int nx = c.nx, ny = c.ny, nz = c.nz;
-  const double hx = 1.0 / nx, hy = 1.0 / ny, hz = 1.0 / nz;
+  const bool ext = c.box_max > c.box_min;
+  const double lo = ext ? c.box_min : 0.0, len = ext ? c.box_max - c.box_min : 1.0;
+  const double hx = len / nx, hy = len / ny, hz = len / nz;
   static const int vi[8] = {0, 1, 1, 0, 0, 1, 1, 0};
   static const int vj[8] = {0, 0, 1, 1, 0, 0, 1, 1};
   static const int vk[8] = {0, 0, 0, 0, 1, 1, 1, 1};
@@ -73,7 +75,7 @@ static void box_vertices(const nekb_bp_config& c, double* EX, double* EY, double
     const int ex = (int)(e % nx), ey = (int)((e / nx) % ny), ez = (int)(e / ((int64_t)nx * ny));
     for (int v = 0; v < 8; ++v) {
       const int I = ex + vi[v], J = ey + vj[v], K = ez + vk[v];
-      double X = I * hx, Y = J * hy, Z = K * hz;
+      double X = lo + I * hx, Y = lo + J * hy, Z = lo + K * hz;
       const bool interior = I > 0 && I < nx && J > 0 && J < ny && K > 0 && K < nz;
       if (interior && !c.periodic && c.perturb != 0.0) {
         const uint64_t vid = (uint64_t)I + (uint64_t)(nx + 1) * ((uint64_t)J + (uint64_t)(ny + 1) * K);

@@ -68,3 +68,8 @@ struct nekb_bp {
   void* net = nullptr;  // learned preconditioner in use (nekb_net*)
   nekb::DeviceBuf net_tmp;
 };
+
+namespace nekb {
+// BPZeroMean (nekBone/solve.cpp:115-134) on the problem's stream, asynchronous
+int bp_zero_mean(nekb_bp* bp, double* q);
+}  // namespace nekb

@@ -24,6 +24,7 @@ int peak_fma(int fp64, double* tflops);
 int peak_copy(double* gbs);
 int bp_weighted_inner_product(nekb_bp* bp, const double* w, const double* a, const double* b,
                               bool two, double* host_out);
+int bp_zero_mean(nekb_bp* bp, double* q);
 }  // namespace nekb
 
 using namespace nekb;
@@ -349,6 +350,13 @@ void nekb_pcg_default_opts(nekb_pcg_opts* o)
   o->max_outer = 20;
   o->check_every = 16;
   o->use_graph = 1;
+}
+
+int nekb_bp_zero_mean(nekb_bp* bp, double* q)
+{
+  NEKB_TRY(bp_zero_mean(bp, q));
+  NEKB_CUDA(cudaStreamSynchronize(bp->stream));
+  return NEKB_OK;
 }
 
 int nekb_bp_pcg(nekb_bp* bp, const double* lambda, double* r, double* x, double tol, int maxit,

@@ -10,7 +10,8 @@
 //   k_net_train : forward, loss, backward-data and weight gradients of a batch
 //                 of elements fused in one kernel; per-block partial gradients.
 //   k_net_reduce: fixed-order sum of the partials (deterministic), then Adam.
-// In the solver: z = invDiag*r + mask(gs(w * s_e * net(r_e/s_e))).
+// In the solver: z = invDiag*r + mask(gs(w * h * s_e * net(h r_e / s_e))),
+// h = sqrt(invDiag) per node, s_e = RMS of h r over element e.
 // No counterpart in the reference.
 #include "nn.h"
 
@@ -25,6 +26,7 @@ struct nekb_net {
   float beta1 = 0.9f, beta2 = 0.999f, eps = 1e-8f;
   nekb::DeviceBuf W, Wbf, m, v, grad, gpart, lpart, loss;
   int gblocks = 0;
+  int inference = NEKB_NET_TENSOR;  // NEKB_NET_TENSOR where built (Nq=8, C=16), else FP32 cores
 };
 
 namespace nekb {
@@ -146,9 +148,11 @@ __device__ void load_weights(const TW* W, float* sW, int C)
   }
 }
 
-// normalize: input r_e / s_e with s_e = RMS(r_e); output times w * s_e * d_e,
-// d_e = mean of invDiag over the element (1 without invDiag), which makes the
-// learned map independent of the mesh size h.
+// normalize: input h r_e / s_e with h = sqrt(invDiag) per node (1 without
+// invDiag) and s_e = RMS of h r_e; output times w * h * s_e.  The symmetric
+// diagonal scaling makes the map the network has to represent nearly uniform
+// across the GLL nodes (whose weights span three decades at N=7) and
+// independent of the element size.
 template <int NQ, int C>
 __global__ void __launch_bounds__(threads_of(NQ))
 k_net_infer(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ Wbf,
@@ -170,10 +174,10 @@ k_net_infer(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ Wbf,
   const int i = n % NQ, j = (n / NQ) % NQ, k = n / (NQ * NQ);
   const unsigned msk = act ? tap_mask<NQ>(i, j, k) : 0u;
   for (int64_t e = blockIdx.x; e < Etot; e += gridDim.x) {
-    const float v = act ? r[e * NP + n] : 0.f;
-    float s = 1.f, dmean = 1.f;
+    const float h = (act && invDiag) ? sqrtf(invDiag[(e % Efield) * NP + n]) : 1.f;
+    const float v = act ? h * r[e * NP + n] : 0.f;
+    float s = 1.f;
     if (normalize) s = sqrtf(block_sum_f(v * v, red) / NP);
-    if (invDiag) dmean = block_sum_f(act ? invDiag[(e % Efield) * NP + n] : 0.f, red) / NP;
     const float inv = s > 0.f ? 1.f / s : 0.f;
     if (act) a0[n] = v * inv;
     __syncthreads();
@@ -195,7 +199,7 @@ k_net_infer(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ Wbf,
       float acc[1];
       conv_fwd<NQ, C, 1>(a2, sW + o3, n, msk, acc);
       const float wn = w ? w[(e % Efield) * NP + n] : 1.f;
-      out[e * NP + n] = wn * s * dmean * acc[0];
+      out[e * NP + n] = wn * h * s * acc[0];
     }
     __syncthreads();
   }
@@ -383,8 +387,8 @@ __global__ void k_net_combine(int64_t N, int64_t Nloc, const float* __restrict__
     z[n] = zn[n] + invDiag[n % Nloc] * r[n];
 }
 
-// in = r_e / s_e ; target = (e_e - invDiag r_e) / (s_e d_e), s_e = RMS of r over element e,
-// d_e = mean invDiag over the element (1 without invDiag)
+// in = h r_e / s_e ; target = (e_e - invDiag r_e) / (h s_e), h = sqrt(invDiag) per node
+// (1 without invDiag), s_e = RMS of h r over element e
 __global__ void k_prepare_pairs(int Np, int64_t Efield, const float* __restrict__ r,
                                 const float* __restrict__ err, const float* __restrict__ invDiag,
                                 float* __restrict__ in, float* __restrict__ target)
@@ -393,21 +397,143 @@ __global__ void k_prepare_pairs(int Np, int64_t Efield, const float* __restrict_
   const int64_t e = blockIdx.x;
   float ss = 0.f;
   for (int n = threadIdx.x; n < Np; n += blockDim.x) {
-    const float v = r[e * Np + n];
+    const float h = invDiag ? sqrtf(invDiag[(e % Efield) * Np + n]) : 1.f;
+    const float v = h * r[e * Np + n];
     ss += v * v;
   }
   const float s = sqrtf(block_sum_f(ss, red) / Np);
-  float ds = 0.f;
-  for (int n = threadIdx.x; n < Np; n += blockDim.x) ds += invDiag ? invDiag[(e % Efield) * Np + n] : 0.f;
-  const float dmean = invDiag ? block_sum_f(ds, red) / Np : 1.f;
   const float inv = s > 0.f ? 1.f / s : 0.f;
-  const float tinv = (s > 0.f && dmean > 0.f) ? 1.f / (s * dmean) : 0.f;
   for (int n = threadIdx.x; n < Np; n += blockDim.x) {
     const int64_t id = e * Np + n;
+    const float d = invDiag ? invDiag[(e % Efield) * Np + n] : 1.f;
+    const float h = invDiag ? sqrtf(d) : 1.f;
     const float rv = r[id];
-    const float dj = invDiag ? invDiag[(e % Efield) * Np + n] * rv : 0.f;
-    in[id] = rv * inv;
-    target[id] = (err[id] - dj) * tinv;
+    const float dj = invDiag ? d * rv : 0.f;
+    in[id] = h * rv * inv;
+    target[id] = (h > 0.f && s > 0.f) ? (err[id] - dj) / (h * s) : 0.f;
+  }
+}
+
+// Element-local correction of a residual: on each element's interior nodes
+// (not shared with any other element) the solution y of the element Helmholtz
+// problem A_II y = r_I with y = 0 on the element boundary (CG in FP32, one CTA
+// per element, thread (i,j) owns the k-column); on the element-boundary nodes
+// the Jacobi value invDiag * r.  This block solve is the linear map a local
+// network can represent; PCG with it takes ~1.6x fewer iterations than Jacobi.
+template <int NQ>
+__host__ __device__ constexpr int lc_threads() { return (NQ * NQ + 31) / 32 * 32; }
+
+template <int NQ>
+__global__ void __launch_bounds__(lc_threads<NQ>())
+k_local_correction(int64_t Esel, int64_t E, const int32_t* __restrict__ elems, const double* __restrict__ ggeo,
+                   const float* __restrict__ Dg, const double* __restrict__ lambda, int64_t offset,
+                   const float* __restrict__ r, const float* __restrict__ invDiag,
+                   float* __restrict__ y, int iters, float tol)
+{
+  constexpr int NQ2 = NQ * NQ, NP = NQ2 * NQ, NW = lc_threads<NQ>() / 32;
+  __shared__ float sD[NQ][NQ], sp[NP], sGr[NP], sGs[NP];
+  __shared__ float red[NW];
+  const int tid = threadIdx.x;
+  const bool act = tid < NQ2;                 // lanes past the face only join the sums
+  const int ij = act ? tid : 0, i = ij % NQ, j = ij / NQ;
+  for (int t = tid; t < NQ2; t += blockDim.x) sD[t / NQ][t % NQ] = Dg[t];
+  const bool ij_int = act && i > 0 && i < NQ - 1 && j > 0 && j < NQ - 1;
+  auto bsum = [&](float v) {  // block sum in a fixed order
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if ((tid & 31) == 0) red[tid >> 5] = v;
+    __syncthreads();
+    float s = 0.f;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) s += red[w];
+    return s;
+  };
+  for (int64_t b = blockIdx.x; b < Esel; b += gridDim.x) {
+    const int64_t e = elems[b];
+    if (e < 0 || e >= E) {  // not an element of this mesh: the row is left as zeros
+      if (act)
+        for (int k = 0; k < NQ; ++k) y[b * NP + k * NQ2 + ij] = 0.f;
+      continue;
+    }
+    const double* g = ggeo + e * 7 * NP + ij;
+    float G[7][NQ], l0[NQ], l1[NQ], rr_[NQ], x[NQ], res[NQ], p[NQ], Ap[NQ];
+    bool in_k[NQ];
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+#pragma unroll
+      for (int sl = 0; sl < 7; ++sl) G[sl][k] = (float)g[sl * NP + k * NQ2];
+      l0[k] = (float)lambda[e * NP + k * NQ2 + ij];
+      l1[k] = (float)lambda[e * NP + k * NQ2 + ij + offset];
+      in_k[k] = ij_int && k > 0 && k < NQ - 1;
+      rr_[k] = r[b * NP + k * NQ2 + ij];
+      x[k] = 0.f;
+      res[k] = in_k[k] ? rr_[k] : 0.f;
+      p[k] = res[k];
+    }
+    float rho = 0.f;
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) rho += res[k] * res[k];
+    rho = bsum(rho);
+    const float rho0 = rho;
+    for (int it = 0; it < iters && rho > tol * tol * rho0 && rho > 0.f; ++it) {
+      // Ap = A p on the element, restricted to its interior nodes
+      if (act) {
+#pragma unroll
+        for (int k = 0; k < NQ; ++k) sp[k * NQ2 + ij] = p[k];
+      }
+      __syncthreads();
+      float gt[NQ];
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) {
+        float qr = 0.f, qs = 0.f, qt = 0.f;
+#pragma unroll
+        for (int m = 0; m < NQ; ++m) {
+          qr += sD[i][m] * sp[k * NQ2 + j * NQ + m];
+          qs += sD[j][m] * sp[k * NQ2 + m * NQ + i];
+          qt += sD[k][m] * p[m];
+        }
+        if (act) {
+          sGr[k * NQ2 + ij] = l0[k] * (G[1][k] * qr + G[2][k] * qs + G[3][k] * qt);
+          sGs[k * NQ2 + ij] = l0[k] * (G[2][k] * qr + G[4][k] * qs + G[5][k] * qt);
+        }
+        gt[k] = l0[k] * (G[3][k] * qr + G[5][k] * qs + G[6][k] * qt);
+      }
+      __syncthreads();
+      float pAp = 0.f;
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) {
+        float ak = G[0][k] * l1[k] * p[k];
+#pragma unroll
+        for (int m = 0; m < NQ; ++m)
+          ak += sD[m][i] * sGr[k * NQ2 + j * NQ + m] + sD[m][j] * sGs[k * NQ2 + m * NQ + i] +
+                sD[m][k] * gt[m];
+        Ap[k] = in_k[k] ? ak : 0.f;
+        pAp += p[k] * Ap[k];
+      }
+      pAp = bsum(pAp);
+      const float alpha = pAp > 0.f ? rho / pAp : 0.f;
+      float rho1 = 0.f;
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) {
+        x[k] += alpha * p[k];
+        res[k] -= alpha * Ap[k];
+        rho1 += res[k] * res[k];
+      }
+      rho1 = bsum(rho1);
+      const float beta = rho1 / rho;
+      rho = pAp > 0.f ? rho1 : 0.f;
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) p[k] = res[k] + beta * p[k];
+    }
+    if (act) {
+#pragma unroll
+      for (int k = 0; k < NQ; ++k) {
+        const int64_t id = b * NP + k * NQ2 + ij;
+        y[id] = in_k[k] ? x[k] : invDiag[id] * rr_[k];
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -477,6 +603,9 @@ int run_train(nekb_net* net, int64_t E, const float* in, const float* target, cu
 int net_infer(const nekb_net* net, int64_t Etot, int64_t Efield, const float* r, const float* w,
               const float* invDiag, float* out, int normalize, const int* skip, cudaStream_t s)
 {
+  if (net->inference == NEKB_NET_TENSOR && net_tc_supported(net->Nq, net->C))
+    return net_infer_tc(net->Wbf.as<__nv_bfloat16>(), Etot, Efield, r, w, invDiag, out, normalize,
+                        skip, s);
   NEKB_NET_DISPATCH(run_infer, net, Etot, Efield, r, w, invDiag, out, normalize, skip, s)
 }
 
@@ -548,6 +677,17 @@ static int net_upload(nekb_net* net, const float* w)
   return NEKB_OK;
 }
 
+template <int NQ>
+static void launch_local_correction(int64_t n, const int32_t* elems, const nekb_bp* bp,
+                                    const double* lambda, const float* r, const float* invDiag,
+                                    float* y, int iters, float tol, cudaStream_t s)
+{
+  const unsigned g = (unsigned)std::min<int64_t>(n, 152 * 32);
+  k_local_correction<NQ><<<g, lc_threads<NQ>(), 0, s>>>(
+      n, bp->E, elems, bp->ggeo.as<double>(), bp->Df.as<float>(), lambda, bp->offset, r, invDiag, y,
+      iters, tol);
+}
+
 extern "C" {
 
 nekb_net* nekb_net_create(int Nq, int channels, int layers, uint64_t seed, int* status)
@@ -584,6 +724,21 @@ nekb_net* nekb_net_create(int Nq, int channels, int layers, uint64_t seed, int* 
 }
 
 void nekb_net_free(nekb_net* net) { delete net; }
+
+int nekb_net_set_inference(nekb_net* net, int mode)
+{
+  if (!net || (mode != NEKB_NET_FP32 && mode != NEKB_NET_TENSOR))
+    return fail(NEKB_ERR_INVALID, "net inference: bad handle or mode %d", mode);
+  net->inference = mode;
+  return NEKB_OK;
+}
+
+int nekb_net_inference(const nekb_net* net)
+{
+  if (!net) return fail(NEKB_ERR_INVALID, "net inference: NULL handle");
+  return (net->inference == NEKB_NET_TENSOR && net_tc_supported(net->Nq, net->C)) ? NEKB_NET_TENSOR
+                                                                                  : NEKB_NET_FP32;
+}
 
 int nekb_net_num_params(const nekb_net* net) { return net ? net->P : 0; }
 
@@ -649,6 +804,29 @@ int nekb_net_prepare_pairs(int Np, int64_t E, int64_t Efield, const float* r, co
   if (E > 0x7fffffff) return fail(NEKB_ERR_INVALID, "prepare pairs: too many elements");
   k_prepare_pairs<<<(unsigned)E, 256, 0, static_cast<cudaStream_t>(stream)>>>(Np, Efield, r, err, invDiag, in, target);
   NEKB_CUDA(cudaGetLastError());
+  return NEKB_OK;
+}
+
+int nekb_bp_local_correction(nekb_bp* bp, const double* lambda, const int32_t* elems, int64_t n,
+                             const float* r, const float* invDiag, float* y, int iters, float tol)
+{
+  if (!bp || n < 0 || iters < 0 || !(tol >= 0.f) ||
+      (n > 0 && (!lambda || !elems || !r || !invDiag || !y)))
+    return fail(NEKB_ERR_INVALID, "local correction: bad arguments");
+  if (n == 0) return NEKB_OK;
+  cudaStream_t s = bp->stream;
+  switch (bp->Nq) {
+    case 3: launch_local_correction<3>(n, elems, bp, lambda, r, invDiag, y, iters, tol, s); break;
+    case 4: launch_local_correction<4>(n, elems, bp, lambda, r, invDiag, y, iters, tol, s); break;
+    case 5: launch_local_correction<5>(n, elems, bp, lambda, r, invDiag, y, iters, tol, s); break;
+    case 6: launch_local_correction<6>(n, elems, bp, lambda, r, invDiag, y, iters, tol, s); break;
+    case 7: launch_local_correction<7>(n, elems, bp, lambda, r, invDiag, y, iters, tol, s); break;
+    case 8: launch_local_correction<8>(n, elems, bp, lambda, r, invDiag, y, iters, tol, s); break;
+    default:
+      return fail(NEKB_ERR_UNSUPPORTED, "local correction: Nq=%d not built (3..8)", bp->Nq);
+  }
+  NEKB_CUDA(cudaGetLastError());
+  NEKB_CUDA(cudaStreamSynchronize(s));
   return NEKB_OK;
 }
 

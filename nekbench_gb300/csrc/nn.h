@@ -3,11 +3,20 @@
 
 #include "bp.h"
 
+#include <cuda_bf16.h>
+
 namespace nekb {
 
-// z = Jacobi(r) + mask(gs(w * s_e * net(r_e / s_e))), s_e = RMS of r over element e.
+// z = Jacobi(r) + mask(gs(w * h * s_e * net(h * r_e / s_e))), h = sqrt(invDiag),
+// s_e = RMS of h * r over element e.
 // Runs on stream s; returns at once on the device when *skip != 0.
 int net_precondition(nekb_bp* bp, nekb_net* net, const float* r, float* z, const float* invDiag,
                      const float* w, const int* skip, cudaStream_t s);
+
+// tensor-core inference (nn_tc.cu): Nq=8, 16 channels
+bool net_tc_supported(int Nq, int C);
+int net_infer_tc(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const float* r,
+                 const float* w, const float* invDiag, float* out, int normalize, const int* skip,
+                 cudaStream_t s);
 
 }  // namespace nekb

@@ -169,8 +169,30 @@ __device__ void state_refresh(PcgState* st, double rz, double rr, double zAp)
   st->beta = beta;
 }
 
+// V consecutive entries per access: V = 4 (float4) for FP32 vectors whose
+// length and field offset are multiples of 4, else 1
+template <int V, typename T>
+__device__ __forceinline__ void vld(const T* p, T (&v)[V])
+{
+  if constexpr (V == 4) {
+    const float4 t = *reinterpret_cast<const float4*>(p);
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+  } else {
+    v[0] = *p;
+  }
+}
+template <int V, typename T>
+__device__ __forceinline__ void vst(T* p, const T (&v)[V])
+{
+  if constexpr (V == 4) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  } else {
+    *p = v[0];
+  }
+}
+
 // [x += alpha p; r -= alpha Ap;] z = M r; sums w r z, w r r (, w z Ap)
-template <typename T, int MODE, bool UPDATE, bool FLEX, bool REFRESH = false>
+template <typename T, int MODE, bool UPDATE, bool FLEX, bool REFRESH = false, int V = 1>
 __global__ void __launch_bounds__(RT) k_update_rz(PcgArgs<T> a)
 {
   PcgState* st = a.st;
@@ -178,31 +200,45 @@ __global__ void __launch_bounds__(RT) k_update_rz(PcgArgs<T> a)
   const T alpha = UPDATE ? (T)st->alpha : T(0);
   T rz = 0, rr = 0, za = 0;
   const int64_t stride = (int64_t)gridDim.x * RT;
+  const int64_t nv = a.Nloc / V;
   for (int f = 0; f < a.NF; ++f) {
     const int64_t fo = f * a.offset;
-    for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < a.Nloc; i += stride) {
-      const int64_t n = i + fo;
-      T r = a.r[n];
-      T ap = T(0);
-      if (UPDATE || FLEX) ap = a.Ap[n];
+    for (int64_t iv = (int64_t)blockIdx.x * RT + threadIdx.x; iv < nv; iv += stride) {
+      const int64_t i = iv * V, n = i + fo;
+      T r[V], ap[V], z[V], w[V];
+      vld<V>(a.r + n, r);
+      if (UPDATE || FLEX) vld<V>(a.Ap + n, ap);
       if (UPDATE) {
-        a.x[n] += alpha * a.p[n];
-        r -= alpha * ap;
-        a.r[n] = r;
+        T x[V], p[V];
+        vld<V>(a.x + n, x);
+        vld<V>(a.p + n, p);
+#pragma unroll
+        for (int l = 0; l < V; ++l) {
+          x[l] += alpha * p[l];
+          r[l] -= alpha * ap[l];
+        }
+        vst<V>(a.x + n, x);
+        vst<V>(a.r + n, r);
       }
-      T z;
       if (MODE == PC_COPY) {
-        z = r;
+#pragma unroll
+        for (int l = 0; l < V; ++l) z[l] = r[l];
       } else if (MODE == PC_JACOBI) {
-        z = a.invDiag[i] * r;
-        a.z[n] = z;
+        T d[V];
+        vld<V>(a.invDiag + i, d);
+#pragma unroll
+        for (int l = 0; l < V; ++l) z[l] = d[l] * r[l];
+        vst<V>(a.z + n, z);
       } else {
-        z = a.z[n];
+        vld<V>(a.z + n, z);
       }
-      const T w = a.w[i];
-      rz += w * r * z;
-      rr += w * r * r;
-      if (FLEX) za += w * z * ap;
+      vld<V>(a.w + i, w);
+#pragma unroll
+      for (int l = 0; l < V; ++l) {
+        rz += w[l] * r[l] * z[l];
+        rr += w[l] * r[l] * r[l];
+        if (FLEX) za += w[l] * z[l] * ap[l];
+      }
     }
   }
   double v[3] = {(double)rz, (double)rr, (double)za};
@@ -228,29 +264,42 @@ __global__ void __launch_bounds__(RT) k_update(PcgArgs<T> a)
 }
 
 // p = z + beta p   (z = r for the COPY preconditioner)
-template <typename T, int MODE>
+template <typename T, int MODE, int V = 1>
 __global__ void __launch_bounds__(RT) k_pupdate(PcgArgs<T> a)
 {
   if (a.st->done) return;
   const T beta = (T)a.st->beta;
   const T* zs = (MODE == PC_COPY) ? a.r : a.z;
-  const int64_t N = a.NF * a.offset;
-  for (int64_t n = (int64_t)blockIdx.x * RT + threadIdx.x; n < N; n += (int64_t)gridDim.x * RT)
-    a.p[n] = zs[n] + beta * a.p[n];
+  const int64_t N = a.NF * a.offset / V;
+  for (int64_t nv = (int64_t)blockIdx.x * RT + threadIdx.x; nv < N; nv += (int64_t)gridDim.x * RT) {
+    T z[V], p[V];
+    vld<V>(zs + nv * V, z);
+    vld<V>(a.p + nv * V, p);
+#pragma unroll
+    for (int l = 0; l < V; ++l) p[l] = z[l] + beta * p[l];
+    vst<V>(a.p + nv * V, p);
+  }
 }
 
 // pAp = sum w p Ap ; alpha = rdotz / pAp
-template <typename T>
+template <typename T, int V = 1>
 __global__ void __launch_bounds__(RT) k_pap(PcgArgs<T> a)
 {
   PcgState* st = a.st;
   if (st->done) return;
   T acc = 0;
   const int64_t stride = (int64_t)gridDim.x * RT;
+  const int64_t nv = a.Nloc / V;
   for (int f = 0; f < a.NF; ++f) {
     const int64_t fo = f * a.offset;
-    for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < a.Nloc; i += stride)
-      acc += a.w[i] * a.p[i + fo] * a.Ap[i + fo];
+    for (int64_t iv = (int64_t)blockIdx.x * RT + threadIdx.x; iv < nv; iv += stride) {
+      T w[V], p[V], ap[V];
+      vld<V>(a.w + iv * V, w);
+      vld<V>(a.p + iv * V + fo, p);
+      vld<V>(a.Ap + iv * V + fo, ap);
+#pragma unroll
+      for (int l = 0; l < V; ++l) acc += w[l] * p[l] * ap[l];
+    }
   }
   double v[1] = {(double)acc};
   if (grid_sum<1>(v, a.partials, a.counter)) {
@@ -387,72 +436,94 @@ struct ExtPrecond {
   const float* w = nullptr;
 };
 
+// float4 access when the vectors allow it (FP32, lengths and offsets multiples of 4)
+template <typename T>
+inline int vec_width(const PcgArgs<T>& a)
+{
+  return (sizeof(T) == 4 && a.Nloc % 4 == 0 && a.offset % 4 == 0) ? 4 : 1;
+}
+
+template <typename T, int MODE, bool UPDATE, bool REFRESH, int V>
+void launch_rz_v(const PcgArgs<T>& a, bool flex, cudaStream_t s)
+{
+  const unsigned rg = red_grid(a.Nloc / V);
+  if (flex)
+    k_update_rz<T, MODE, UPDATE, true, REFRESH, V><<<rg, RT, 0, s>>>(a);
+  else
+    k_update_rz<T, MODE, UPDATE, false, REFRESH, V><<<rg, RT, 0, s>>>(a);
+}
+
+// k_update_rz for the runtime (mode, flex) pair and vector width
+template <typename T, bool UPDATE, bool REFRESH>
+int launch_rz(const PcgArgs<T>& a, int mode, bool flex, cudaStream_t s)
+{
+  const bool v4 = vec_width(a) == 4;
+  if constexpr (sizeof(T) == 4) {
+    if (v4) {
+      if (mode == PC_EXTERNAL) launch_rz_v<T, PC_EXTERNAL, UPDATE, REFRESH, 4>(a, flex, s);
+      else if (mode == PC_JACOBI) launch_rz_v<T, PC_JACOBI, UPDATE, REFRESH, 4>(a, flex, s);
+      else launch_rz_v<T, PC_COPY, UPDATE, REFRESH, 4>(a, flex, s);
+      NEKB_CUDA(cudaGetLastError());
+      return NEKB_OK;
+    }
+  }
+  if (mode == PC_EXTERNAL) launch_rz_v<T, PC_EXTERNAL, UPDATE, REFRESH, 1>(a, flex, s);
+  else if (mode == PC_JACOBI) launch_rz_v<T, PC_JACOBI, UPDATE, REFRESH, 1>(a, flex, s);
+  else launch_rz_v<T, PC_COPY, UPDATE, REFRESH, 1>(a, flex, s);
+  NEKB_CUDA(cudaGetLastError());
+  return NEKB_OK;
+}
+
 template <typename T>
 int launch_iteration(const OpView& op, PcgArgs<T> a, int mode, bool flex, const ExtPrecond* ext,
                      cudaStream_t s)
 {
   const int64_t Nall = a.NF * a.offset;
-  const unsigned vg = vec_grid(Nall), rg = red_grid(a.Nloc);
-  if (mode == PC_COPY)
-    k_pupdate<T, PC_COPY><<<vg, RT, 0, s>>>(a);
-  else
-    k_pupdate<T, PC_JACOBI><<<vg, RT, 0, s>>>(a);
+  const int V = vec_width(a);
+  const unsigned vg = vec_grid(Nall / V), rg = red_grid(a.Nloc / V);
+  if constexpr (sizeof(T) == 4) {
+    if (V == 4) {
+      if (mode == PC_COPY)
+        k_pupdate<T, PC_COPY, 4><<<vg, RT, 0, s>>>(a);
+      else
+        k_pupdate<T, PC_JACOBI, 4><<<vg, RT, 0, s>>>(a);
+    }
+  }
+  if (V == 1) {
+    if (mode == PC_COPY)
+      k_pupdate<T, PC_COPY, 1><<<vg, RT, 0, s>>>(a);
+    else
+      k_pupdate<T, PC_JACOBI, 1><<<vg, RT, 0, s>>>(a);
+  }
   NEKB_CUDA(cudaGetLastError());
   NEKB_TRY(apply_op(op, a.p, a.Ap, &a.st->done, s));
-  k_pap<T><<<rg, RT, 0, s>>>(a);
+  if constexpr (sizeof(T) == 4) {
+    if (V == 4) k_pap<T, 4><<<rg, RT, 0, s>>>(a);
+  }
+  if (V == 1) k_pap<T, 1><<<rg, RT, 0, s>>>(a);
   NEKB_CUDA(cudaGetLastError());
   if (mode == PC_EXTERNAL) {
-    k_update<T><<<vg, RT, 0, s>>>(a);
+    k_update<T><<<vec_grid(Nall), RT, 0, s>>>(a);
     NEKB_CUDA(cudaGetLastError());
     if constexpr (sizeof(T) == 4) {
       NEKB_TRY(net_precondition(ext->bp, ext->net, a.r, a.z, ext->invDiag, ext->w, &a.st->done, s));
     } else {
       return fail(NEKB_ERR_UNSUPPORTED, "learned preconditioner runs in FP32 only");
     }
-    if (flex)
-      k_update_rz<T, PC_EXTERNAL, false, true><<<rg, RT, 0, s>>>(a);
-    else
-      k_update_rz<T, PC_EXTERNAL, false, false><<<rg, RT, 0, s>>>(a);
-  } else if (mode == PC_JACOBI) {
-    if (flex)
-      k_update_rz<T, PC_JACOBI, true, true><<<rg, RT, 0, s>>>(a);
-    else
-      k_update_rz<T, PC_JACOBI, true, false><<<rg, RT, 0, s>>>(a);
-  } else {
-    if (flex)
-      k_update_rz<T, PC_COPY, true, true><<<rg, RT, 0, s>>>(a);
-    else
-      k_update_rz<T, PC_COPY, true, false><<<rg, RT, 0, s>>>(a);
+    return launch_rz<T, false, false>(a, mode, flex, s);
   }
-  NEKB_CUDA(cudaGetLastError());
-  return NEKB_OK;
+  return launch_rz<T, true, false>(a, mode, flex, s);
 }
 
 template <typename T>
 int launch_first_rz(PcgArgs<T> a, int mode, bool flex, const ExtPrecond* ext, cudaStream_t s)
 {
-  const unsigned rg = red_grid(a.Nloc);
   if (mode == PC_EXTERNAL) {
     if constexpr (sizeof(T) == 4) {
       NEKB_TRY(net_precondition(ext->bp, ext->net, a.r, a.z, ext->invDiag, ext->w, &a.st->done, s));
     }
-    if (flex)
-      k_update_rz<T, PC_EXTERNAL, false, true><<<rg, RT, 0, s>>>(a);
-    else
-      k_update_rz<T, PC_EXTERNAL, false, false><<<rg, RT, 0, s>>>(a);
-  } else if (mode == PC_JACOBI) {
-    if (flex)
-      k_update_rz<T, PC_JACOBI, false, true><<<rg, RT, 0, s>>>(a);
-    else
-      k_update_rz<T, PC_JACOBI, false, false><<<rg, RT, 0, s>>>(a);
-  } else {
-    if (flex)
-      k_update_rz<T, PC_COPY, false, true><<<rg, RT, 0, s>>>(a);
-    else
-      k_update_rz<T, PC_COPY, false, false><<<rg, RT, 0, s>>>(a);
   }
-  NEKB_CUDA(cudaGetLastError());
-  return NEKB_OK;
+  return launch_rz<T, false, false>(a, mode, flex, s);
 }
 
 template <typename T>
@@ -478,28 +549,12 @@ int wdot(nekb_bp* bp, const T* w, const T* u, const T* v, int NF, double* result
 template <typename T>
 int launch_refresh_rz(PcgArgs<T> a, int mode, bool flex, const ExtPrecond* ext, cudaStream_t s)
 {
-  const unsigned rg = red_grid(a.Nloc);
   if (mode == PC_EXTERNAL) {
     if constexpr (sizeof(T) == 4) {
       NEKB_TRY(net_precondition(ext->bp, ext->net, a.r, a.z, ext->invDiag, ext->w, &a.st->done, s));
     }
-    if (flex)
-      k_update_rz<T, PC_EXTERNAL, false, true, true><<<rg, RT, 0, s>>>(a);
-    else
-      k_update_rz<T, PC_EXTERNAL, false, false, true><<<rg, RT, 0, s>>>(a);
-  } else if (mode == PC_JACOBI) {
-    if (flex)
-      k_update_rz<T, PC_JACOBI, false, true, true><<<rg, RT, 0, s>>>(a);
-    else
-      k_update_rz<T, PC_JACOBI, false, false, true><<<rg, RT, 0, s>>>(a);
-  } else {
-    if (flex)
-      k_update_rz<T, PC_COPY, false, true, true><<<rg, RT, 0, s>>>(a);
-    else
-      k_update_rz<T, PC_COPY, false, false, true><<<rg, RT, 0, s>>>(a);
   }
-  NEKB_CUDA(cudaGetLastError());
-  return NEKB_OK;
+  return launch_rz<T, false, true>(a, mode, flex, s);
 }
 
 // called after every chunk with the state in bp->h_state; sets *finish to end
@@ -915,11 +970,18 @@ int bp_pcg(nekb_bp* bp, const double* lambda, double* r, double* x, double tol, 
   NEKB_CUDA(cudaEventCreate(&e0));
   NEKB_CUDA(cudaEventCreate(&e1));
   NEKB_CUDA(cudaEventRecord(e0, bp->stream));
-  int st;
-  if (o.solver == NEKB_SOLVER_MIXED)
-    st = solve_mixed(bp, lambda, r, x, tol, maxit, o, stats);
-  else
-    st = solve_fp64(bp, lambda, r, x, tol, maxit, o, stats);
+  int st = NEKB_OK;
+  if (o.zero_mean) st = bp_zero_mean(bp, r);  // solve(), nekBone/main.cpp:24-25
+  if (st == NEKB_OK) {
+    if (o.solver == NEKB_SOLVER_MIXED)
+      st = solve_mixed(bp, lambda, r, x, tol, maxit, o, stats);
+    else
+      st = solve_fp64(bp, lambda, r, x, tol, maxit, o, stats);
+  }
+  if (o.zero_mean && st == NEKB_OK) {
+    const int zs = bp_zero_mean(bp, x);  // nekBone/main.cpp:30-31
+    if (zs != NEKB_OK) st = zs;
+  }
   cudaEventRecord(e1, bp->stream);
   cudaEventSynchronize(e1);
   float ms = 0;
@@ -928,6 +990,50 @@ int bp_pcg(nekb_bp* bp, const double* lambda, double* r, double* x, double tol, 
   cudaEventDestroy(e1);
   if (st == NEKB_OK) stats->elapsed_s = ms * 1e-3;
   return st;
+}
+
+namespace {
+
+// sum kernel (utils.okl:212): per node the sum over fields, deterministic grid sum
+__global__ void __launch_bounds__(RT) k_field_sum(int64_t N, int NF, int64_t offset,
+                                                  const double* __restrict__ q, double* partials,
+                                                  unsigned* counter, double* out)
+{
+  double acc = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * RT;
+  for (int64_t i = (int64_t)blockIdx.x * RT + threadIdx.x; i < N; i += stride)
+    for (int f = 0; f < NF; ++f) acc += q[i + f * offset];
+  double v[1] = {acc};
+  if (grid_sum<1>(v, partials, counter)) *out = v[0];
+}
+
+// addScalar (utils.okl:29) of minus the mean
+__global__ void k_sub_mean(int64_t N, const double* __restrict__ sum, double count,
+                           double* __restrict__ q)
+{
+  const double m = -(*sum / count);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < N;
+       i += (int64_t)gridDim.x * blockDim.x)
+    q[i] += m;
+}
+
+}  // namespace
+
+// BPZeroMean (solve.cpp:115-134)
+int bp_zero_mean(nekb_bp* bp, double* q)
+{
+  if (!bp || !q) return fail(NEKB_ERR_INVALID, "zero mean: NULL argument");
+  const int64_t N = bp->E * (int64_t)bp->Np, Nall = bp->Nfields * bp->offset;
+  if (N == 0) return NEKB_OK;
+  double* out = bp->partials.as<double>() + 3 * 4096 + 4;
+  k_field_sum<<<red_grid(N), RT, 0, bp->stream>>>(N, bp->Nfields, bp->offset, q,
+                                                  bp->partials.as<double>(),
+                                                  bp->counter.as<unsigned>() + 12, out);
+  NEKB_CUDA(cudaGetLastError());
+  const unsigned g = (unsigned)std::min<int64_t>((Nall + 255) / 256, 152 * 16);
+  k_sub_mean<<<g, 256, 0, bp->stream>>>(Nall, out, (double)(N * bp->Nfields), q);
+  NEKB_CUDA(cudaGetLastError());
+  return NEKB_OK;
 }
 
 int bp_wdot(nekb_bp* bp, const double* u, const double* v, double* out)

@@ -1,14 +1,18 @@
 """Training and evaluation of the learned element preconditioner.
 
-Data: (residual, correction) pairs that the plain Jacobi-PCG itself produces.
-For each seeded problem (lambda0 = 1, lambda1 = 1 + 0.5 sin(2 pi k.x) with
-k ~ U{1..4}^3, f ~ U[-1,1] assembled), the FP32 Jacobi-PCG iterate x_k after
-k iterations (k in SNAPSHOTS) gives the residual r_k = b - A x_k (FP64) and
-the correction the same PCG makes over its next `horizon` iterations,
-x_{k+horizon} - x_k (a local, smoothing map an element network can learn; the
-remaining global error x* - x_k is available with horizon=0).  A random subset
-of elements of each snapshot becomes training pairs through the library's
-nekb_net_prepare_pairs (element RMS normalisation, Jacobi part removed).
+Data: residuals that the plain Jacobi-PCG itself produces, paired with a
+correction.  For each seeded problem (lambda0 = 1, lambda1 = 1 + 0.5
+sin(2 pi k.x) with k ~ U{1..4}^3, f ~ U[-1,1] assembled), the FP32 Jacobi-PCG
+iterate x_k after k iterations (k in SNAPSHOTS) gives the residual
+r_k = b - A x_k (FP64).  The default correction is the element-local block
+solve of r_k (exact on each element's interior nodes, Jacobi on its boundary),
+a fixed linear map of the element's own residual that a local network can
+represent; the alternative is the correction the same PCG makes over its next
+`horizon` iterations, x_{k+horizon} - x_k (horizon=0: the remaining global
+error x* - x_k), which depends on the residual outside the element.  A random
+subset of elements of each snapshot becomes training pairs through the
+library's nekb_net_prepare_pairs (element RMS normalisation, Jacobi part
+removed).
 
 Training runs the network's own fused forward/backward kernels and Adam
 (nekb_net_train_step); evaluation compares flexible PCG with the network
@@ -45,12 +49,21 @@ def rhs(bp, seed, torch, dev):
     return f
 
 
-def generate_pairs(bp, seeds, torch, dev, frac=0.125, snapshots=SNAPSHOTS, horizon=16, log=None):
+def generate_pairs(bp, seeds, torch, dev, frac=0.125, snapshots=SNAPSHOTS, horizon=16, log=None,
+                   target="local"):
     """Training pairs (inp, target), float32 device tensors of shape [M, Np].
 
-    The correction paired with the residual r_k is x_{k+horizon} - x_k, what
-    the Jacobi-PCG itself adds to its iterate over the next `horizon`
-    iterations (horizon=0: the remaining error x* - x_k)."""
+    target="local": the correction paired with the residual r_k is the
+    element-local block solve of r_k (element-interior Helmholtz solve, Jacobi
+    on the element boundary; nekb_bp_local_correction), a fixed linear map of
+    the element's residual.
+    target="pcg": x_{k+horizon} - x_k, what the Jacobi-PCG itself adds to its
+    iterate over the next `horizon` iterations (horizon=0: the remaining error
+    x* - x_k)."""
+    if target not in ("local", "pcg"):
+        raise ValueError(f"unknown target {target!r}")
+    if target == "local":
+        horizon = 1  # no reference solve needed
     E, Np, L = bp.E, bp.Np, bp.Nlocal
     n_sel = max(1, int(frac * E))
     r = torch.empty(L, dtype=torch.float64, device=dev)
@@ -68,7 +81,7 @@ def generate_pairs(bp, seeds, torch, dev, frac=0.125, snapshots=SNAPSHOTS, horiz
         inv_diag = None
         rng = np.random.default_rng(10_000 + s)
         for k in snapshots:
-            if horizon > 0:
+            if horizon > 0 and target == "pcg":
                 r.copy_(f)
                 xs.zero_()
                 bp.pcg(lam, r, xs, 0.0, k + horizon, solver=nb.SOLVER_MIXED,
@@ -80,8 +93,12 @@ def generate_pairs(bp, seeds, torch, dev, frac=0.125, snapshots=SNAPSHOTS, horiz
                 inv_diag = bp.device_array("invDiag", L, torch.float64).float().view(E, Np)
             idx = torch.from_numpy(rng.choice(E, n_sel, replace=False).astype(np.int64)).to(dev)
             rk = r.float().view(E, Np).index_select(0, idx).contiguous()
-            ek = (xs - x).float().view(E, Np).index_select(0, idx).contiguous()
             dk = inv_diag.index_select(0, idx).contiguous()
+            if target == "local":
+                ek = torch.empty_like(rk)
+                bp.local_correction(lam, idx.to(torch.int32), rk, dk, ek)
+            else:
+                ek = (xs - x).float().view(E, Np).index_select(0, idx).contiguous()
             inp = torch.empty_like(rk)
             tgt = torch.empty_like(rk)
             nb.prepare_pairs(Np, n_sel, n_sel, rk, ek, dk, inp, tgt)
@@ -119,10 +136,11 @@ def train(net, inp, tgt, torch, steps=2000, batch=2048, lr=1e-3, seed=0, log=Non
     return losses
 
 
-def evaluate(bp, net, seeds, torch, dev, tol=1e-8, inner_precision=None):
+def evaluate(bp, net, seeds, torch, dev, tol=1e-8, inner_precision=None, solver=None):
     """Iterations and time to `tol` (true FP64 relative residual) with and without
     the network, on the same problems."""
     inner_precision = nb.FP32_TRILINEAR if inner_precision is None else inner_precision
+    solver = nb.SOLVER_MIXED if solver is None else solver
     r = torch.empty(bp.Nlocal, dtype=torch.float64, device=dev)
     x = torch.empty_like(r)
     rows = []
@@ -136,7 +154,7 @@ def evaluate(bp, net, seeds, torch, dev, tol=1e-8, inner_precision=None):
             for _ in range(2):
                 r.copy_(f)
                 x.zero_()
-                st = bp.pcg(lam, r, x, tol, maxit, solver=nb.SOLVER_MIXED,
+                st = bp.pcg(lam, r, x, tol, maxit, solver=solver,
                             inner_precision=inner_precision, **kw)
                 if best is None or st["elapsed_s"] < best["elapsed_s"]:
                     best = st

@@ -26,8 +26,11 @@ def main(argv=None):
     p.add_argument("--lr", type=float, default=2e-3)
     p.add_argument("--channels", type=int, default=16)
     p.add_argument("--frac", type=float, default=0.125)
+    p.add_argument("--target", choices=("local", "pcg"), default="local",
+                   help="local: element-interior block solve of the residual; "
+                        "pcg: the Jacobi-PCG's own correction over --horizon iterations")
     p.add_argument("--horizon", type=int, default=8,
-                   help="correction = x_{k+horizon} - x_k of the Jacobi-PCG (0: x* - x_k)")
+                   help="target pcg: correction = x_{k+horizon} - x_k (0: x* - x_k)")
     p.add_argument("--out", default=os.path.join(os.path.dirname(os.path.abspath(__file__)),
                                                  "weights", "precond_n7_c16.bin"))
     p.add_argument("--report", default=None)
@@ -48,7 +51,7 @@ def main(argv=None):
     bp = nb.BP(7, a.n, a.n, a.n, perturb=0.1, seed=3)
     net = nb.Net(8, a.channels, 3, seed=1)
     inp, tgt = LP.generate_pairs(bp, range(a.train_seeds), torch, dev, frac=a.frac,
-                                 horizon=a.horizon, log=log)
+                                 horizon=a.horizon, log=log, target=a.target)
     losses = LP.train(net, inp, tgt, torch, steps=a.steps, batch=a.batch, lr=a.lr, log=log)
     del inp, tgt
     torch.cuda.empty_cache()
@@ -56,7 +59,7 @@ def main(argv=None):
     net.save(a.out)
     ev = LP.evaluate(bp, net, range(1000, 1000 + a.eval_seeds), torch, dev)
     report = {"workload": f"N=7, E={a.n}^3={bp.E}, lambda1 = 1 + 0.5 sin(2 pi k.x), k~U{{1..4}}^3",
-              "horizon": a.horizon,
+              "target": a.target, "horizon": a.horizon,
               "train_seeds": a.train_seeds, "eval_seeds": a.eval_seeds, "steps": a.steps,
               "batch": a.batch, "lr": a.lr, "channels": a.channels,
               "loss_first": losses[0], "loss_last": losses[-1],

@@ -51,7 +51,8 @@ def lib():
     L.nekbo_gauss.argtypes = [C.c_int, _d, _d]
     L.nekbo_dmatrix.argtypes = [C.c_int, _d, _d]
     L.nekbo_box_vertices.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_uint64, C.c_int,
-                                     _d, _d, _d]
+                                     C.c_double, C.c_double, _d, _d, _d]
+    L.nekbo_zero_mean.argtypes = [C.c_int64, C.c_int, C.c_int64, _d]
     L.nekbo_box_ids.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _i64]
     L.nekbo_box_mask.restype = C.c_int64
     L.nekbo_box_mask.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, _vp]
@@ -123,7 +124,8 @@ def dmatrix(x: np.ndarray) -> np.ndarray:
 class BoxMesh:
     """Structured box of nx*ny*nz hexes of order N (oracle construction)."""
 
-    def __init__(self, N, nx, ny, nz, perturb=0.1, seed=1, periodic=False, dirichlet=True):
+    def __init__(self, N, nx, ny, nz, perturb=0.1, seed=1, periodic=False, dirichlet=True,
+                 box=(0.0, 0.0)):
         L = lib()
         self.N, self.Nq = N, N + 1
         self.Np = self.Nq ** 3
@@ -133,7 +135,8 @@ class BoxMesh:
         self.D = dmatrix(self.r)
         E8 = self.E * 8
         self.EX, self.EY, self.EZ = np.zeros(E8), np.zeros(E8), np.zeros(E8)
-        L.nekbo_box_vertices(nx, ny, nz, perturb, seed, int(periodic), self.EX, self.EY, self.EZ)
+        L.nekbo_box_vertices(nx, ny, nz, perturb, seed, int(periodic), float(box[0]), float(box[1]),
+                             self.EX, self.EY, self.EZ)
         Nl = self.E * self.Np
         self.ids = np.zeros(Nl, dtype=np.int64)
         L.nekbo_box_ids(N, nx, ny, nz, int(periodic), int(dirichlet), self.ids)
@@ -223,6 +226,13 @@ class BP:
         it = lib().nekbo_pcg(C.byref(self.s), r, x, tol, maxit, precond, int(flexible), int(fixed),
                              _ptr(h))
         return (it, h) if hist else it
+
+
+def zero_mean(q, Nloc, Nfields=1, offset=None):
+    """BPZeroMean restatement, in place on the float64 array q."""
+    offset = Nloc if offset is None else offset
+    lib().nekbo_zero_mean(Nloc, Nfields, offset, q)
+    return q
 
 
 # ----------------------------------------------------------------------------- conv net

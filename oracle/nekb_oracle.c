@@ -149,12 +149,16 @@ void nekbo_dmatrix(int Nq, const double* x, double* D)
 /* ------------------------------------------------------------------------ */
 /* Element e = ex + nx*(ey + ny*ez); vertex order as core/meshSetup.cpp:2363-2410
  * (0:(i,j,k) 1:(i+1,j,k) 2:(i+1,j+1,k) 3:(i,j+1,k), 4..7 the same at k+1).
- * Unit box [0,1]^3; interior vertices moved by U[-perturb*h, perturb*h] per
- * coordinate (random stream 1, counter 3*vertex+c). */
+ * Box [box_min, box_max]^3 ([0,1]^3 when box_max <= box_min; the reference's
+ * default is [-1,1]^3, core/meshSetup.cpp:2316-2353); interior vertices moved
+ * by U[-perturb*h, perturb*h] per coordinate (random stream 1, counter
+ * 3*vertex+c). */
 void nekbo_box_vertices(int nx, int ny, int nz, double perturb, uint64_t seed, int periodic,
-                        double* EX, double* EY, double* EZ)
+                        double box_min, double box_max, double* EX, double* EY, double* EZ)
 {
-  const double hx = 1.0 / nx, hy = 1.0 / ny, hz = 1.0 / nz;
+  const int ext = box_max > box_min;
+  const double lo = ext ? box_min : 0.0, len = ext ? box_max - box_min : 1.0;
+  const double hx = len / nx, hy = len / ny, hz = len / nz;
   const int vi[8] = {0, 1, 1, 0, 0, 1, 1, 0};
   const int vj[8] = {0, 0, 1, 1, 0, 0, 1, 1};
   const int vk[8] = {0, 0, 0, 0, 1, 1, 1, 1};
@@ -164,7 +168,7 @@ void nekbo_box_vertices(int nx, int ny, int nz, double perturb, uint64_t seed, i
         int64_t e = ex + (int64_t)nx * (ey + (int64_t)ny * ez);
         for (int v = 0; v < 8; ++v) {
           int I = ex + vi[v], J = ey + vj[v], K = ez + vk[v];
-          double X = I * hx, Y = J * hy, Z = K * hz;
+          double X = lo + I * hx, Y = lo + J * hy, Z = lo + K * hz;
           int interior = (I > 0 && I < nx && J > 0 && J < ny && K > 0 && K < nz);
           if (interior && !periodic && perturb != 0.0) {
             uint64_t vid = (uint64_t)I + (uint64_t)(nx + 1) * ((uint64_t)J + (uint64_t)(ny + 1) * K);
@@ -614,6 +618,15 @@ void nekbo_bp_apply(const nekbo_bp* bp, const double* q, double* Aq)
 /* BPPCG (nekBone/solve.cpp:44-113) with BPPreconditioner (:167-179),
  * BPWeightedInnerProduct2 (:261-287), BPWeightedInnerProduct (:237-259),
  * BPScaledAdd (:289-293), BPUpdatePCG (:136-142) and updateJacobi (:146-165). */
+void nekbo_zero_mean(int64_t Nloc, int Nfields, int64_t offset, double* q)
+{
+  double sum = 0.0;
+  for (int64_t i = 0; i < Nloc; ++i)
+    for (int f = 0; f < Nfields; ++f) sum += q[i + f * offset];
+  const double mean = sum / (double)(Nloc * Nfields);
+  for (int64_t i = 0; i < Nfields * offset; ++i) q[i] += -mean;
+}
+
 int nekbo_pcg(const nekbo_bp* bp, double* r, double* x, double tol, int maxit, int precond,
               int flexible, int fixed_iterations, double* rdotr_hist)
 {

@@ -40,7 +40,7 @@ void nekbo_dmatrix(int Nq, const double* x, double* D); /* D[i*Nq+m] = l_m'(x_i)
 
 /* ---- box mesh (core/meshSetup.cpp:2265 meshSetupBoxHex3D, :2156 meshPhysicalNodesHex3D) ---- */
 void    nekbo_box_vertices(int nx, int ny, int nz, double perturb, uint64_t seed, int periodic,
-                           double* EX, double* EY, double* EZ);
+                           double box_min, double box_max, double* EX, double* EY, double* EZ);
 void    nekbo_box_ids(int N, int nx, int ny, int nz, int periodic, int dirichlet, int64_t* ids);
 int64_t nekbo_box_mask(int N, int nx, int ny, int nz, int32_t* maskIds /* nullable: count only */);
 void    nekbo_physical_nodes(int N, int64_t E, const double* r1d, const double* EX,
@@ -92,6 +92,10 @@ typedef struct {
  * (iter-1 at exit).  rdotr_hist (nullable, maxit+1 entries) gets rdotr per iteration. */
 int nekbo_pcg(const nekbo_bp* bp, double* r, double* x, double tol, int maxit, int precond,
               int flexible, int fixed_iterations, double* rdotr_hist);
+/* BPZeroMean (nekBone/solve.cpp:115-134): q -= (sum of the Nloc local values
+ * of every field) / (Nloc*Nfields), over all Nfields*offset entries.  The sum
+ * runs in index order (the reference sums 256-wide block partials). */
+void nekbo_zero_mean(int64_t Nloc, int Nfields, int64_t offset, double* q);
 /* operator used by the PCG: Aq = mask(gs(axhelm(q))) */
 void nekbo_bp_apply(const nekbo_bp* bp, const double* q, double* Aq);
 double nekbo_wdot(int64_t N, int Nfields, int64_t offset, const double* w, const double* a,

@@ -3,8 +3,12 @@ oracle's 3D-convolution / GELU restatement (composed as in tests/test_oracle.py,
 whose composition is itself checked by finite differences), training progress,
 checkpoint round trip, and its use inside flexible PCG.
 
-Tolerances: forward 2e-5 relative (BF16 weights are used for inference, so the
-oracle is fed the BF16-rounded weights); gradient 1e-4 relative (FP32)."""
+Tolerances: FP32-core forward 2e-5 relative (BF16 weights are used for
+inference, so the oracle is fed the BF16-rounded weights); tensor-core forward
+1e-2 of the output's max-norm and 2e-3 in RMS (the oracle rounds the input and
+both GELU outputs to BF16 as the kernel does; a different FP32 summation order
+or the hardware tanh can move an activation by one BF16 step); gradient 1e-4
+relative (FP32)."""
 import os
 
 import numpy as np
@@ -28,6 +32,8 @@ def bf16(w):
 def test_forward_matches_oracle(nb, O, dev, Nq, C):
     E = 5
     net = nb.Net(Nq, C, 3, seed=3)
+    net.inference = nb.NET_FP32
+    assert net.inference == nb.NET_FP32
     W = net.weights()
     x = O.uniform(E * Nq ** 3, 4, 1, -1, 1).astype(np.float32)
     out = torch.zeros(E * Nq ** 3, dtype=torch.float32, device=dev)
@@ -105,3 +111,69 @@ def test_flexible_pcg_with_network_converges(nb, O, dev):
     r2, x2 = f.clone(), torch.zeros_like(f)
     st2 = bp.pcg(lam, r2, x2, 1e-8, 2000, solver=nb.SOLVER_MIXED)
     assert float((x - x2).abs().max() / x2.abs().max()) < 1e-6
+
+
+@pytest.mark.parametrize("N", [3, 7])
+def test_local_correction_is_the_element_interior_solve(nb, O, dev, N):
+    """nekb_bp_local_correction against a dense solve of each element's
+    interior block, the element matrix assembled column by column from the
+    oracle's axhelm; Jacobi values on the element boundary; a row whose element
+    index is outside the mesh comes back zero.  Tolerance 1e-3 relative (FP32 CG
+    to a relative residual of 1e-6)."""
+    Nq = N + 1
+    Np = Nq ** 3
+    bp = nb.BP(N, 2, 2, 2, perturb=0.15, seed=5)
+    E, L = bp.E, bp.Nlocal
+    lam = np.concatenate([0.5 + O.uniform(L, 21, 1), 1.0 + O.uniform(L, 21, 2)])
+    lam_d = torch.from_numpy(lam).to(dev)
+    elems = np.array([0, 5, 7, 3, E], dtype=np.int32)
+    n = len(elems)
+    r = O.uniform(n * Np, 22, 1, -1, 1).astype(np.float32)
+    dinv = (0.1 + O.uniform(n * Np, 22, 2)).astype(np.float32)
+    y = torch.full((n * Np,), 7.0, dtype=torch.float32, device=dev)
+    bp.local_correction(lam_d, torch.from_numpy(elems).to(dev), torch.from_numpy(r).to(dev),
+                        torch.from_numpy(dinv).to(dev), y, iters=500, tol=1e-6)
+    torch.cuda.synchronize()
+    got = y.cpu().numpy().reshape(n, Np)
+    ggeo = bp.device_array("ggeo", 7 * L, torch.float64).cpu().numpy()
+    D = O.dmatrix(O.gll(N)[0])
+    ii = np.arange(Nq)
+    I3 = np.stack(np.meshgrid(ii, ii, ii, indexing="ij"), -1).reshape(-1, 3)[:, ::-1]  # (i,j,k)
+    interior = np.all((I3 > 0) & (I3 < N), axis=1)
+    for b, e in enumerate(elems[:-1]):
+        ge = ggeo[e * 7 * Np:(e + 1) * 7 * Np]
+        le = np.concatenate([lam[e * Np:(e + 1) * Np], lam[L + e * Np:L + (e + 1) * Np]])
+        A = np.stack([O.axhelm(Nq, 1, Np, 0, ge, D, le, np.eye(Np)[c]) for c in range(Np)], 1)
+        rb = r[b * Np:(b + 1) * Np].astype(np.float64)
+        want = dinv[b * Np:(b + 1) * Np] * rb
+        want[interior] = np.linalg.solve(A[np.ix_(interior, interior)], rb[interior])
+        assert np.abs(got[b] - want).max() <= 1e-3 * np.abs(want).max(), (N, b)
+    assert np.all(got[-1] == 0.0)
+
+
+@pytest.mark.parametrize("seed", [3, 4])
+def test_tensor_core_forward_matches_oracle(nb, O, dev, seed):
+    Nq, C, E = 8, 16, 37
+    net = nb.Net(Nq, C, 3, seed=seed)
+    assert net.inference == nb.NET_TENSOR
+    W = bf16(net.weights())
+    x = O.uniform(E * Nq ** 3, 40 + seed, 1, -1, 1).astype(np.float32)
+    out = torch.zeros(E * Nq ** 3, dtype=torch.float32, device=dev)
+    net.forward(torch.from_numpy(x).to(dev), out, E)
+    torch.cuda.synchronize()
+    o2, o3 = 27 * C, 27 * C + 27 * C * C
+    a1 = bf16(O.gelu(O.conv3d_forward(Nq, W[:o2], bf16(x), 1, C)))
+    a2 = bf16(O.gelu(O.conv3d_forward(Nq, W[o2:o3], a1, C, C)))
+    ref = O.conv3d_forward(Nq, W[o3:], a2, C, 1).astype(np.float64)
+    d = out.cpu().numpy().astype(np.float64) - ref
+    assert np.abs(d).max() <= 1e-2 * np.abs(ref).max()
+    assert np.sqrt(np.mean(d * d)) <= 2e-3 * np.sqrt(np.mean(ref * ref))
+
+
+def test_inference_mode_falls_back_where_not_built(nb):
+    net = nb.Net(4, 8, 3, seed=1)
+    assert net.inference == nb.NET_FP32
+    net.inference = nb.NET_TENSOR
+    assert net.inference == nb.NET_FP32
+    with pytest.raises(nb.NekbError):
+        net.inference = 7

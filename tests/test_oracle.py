@@ -225,3 +225,41 @@ def test_gelu_oracle():
     gx = O.gelu_backward(x, np.ones_like(x))
     fd = (O.gelu(x + 1e-3) - O.gelu(x - 1e-3)) / 2e-3
     assert np.abs(gx - fd).max() < 5e-3
+
+
+def _reference_mode_problem(nx, ny, nz):
+    """nekBone BP mode (nekBone/setup.cpp:44-53, 76-98): periodic unperturbed box
+    [-1,1]^3, N=7, Poisson (BK), rhs 3 pi^2 JW cos(pi x) cos(pi y) cos(pi z)
+    assembled by gather-scatter, COPY preconditioner."""
+    m = O.BoxMesh(7, nx, ny, nz, perturb=0.0, periodic=True, dirichlet=False, box=(-1.0, 1.0))
+    L = m.E * m.Np
+    JW = m.ggeo.reshape(m.E, 7, m.Np)[:, 0, :].reshape(-1)
+    exact = np.cos(np.pi * m.x) * np.cos(np.pi * m.y) * np.cos(np.pi * m.z)
+    bp = O.BP(m, np.concatenate([np.ones(L), np.zeros(L)]), bk=True)
+    r = O.gs_many_add(bp.Ng, bp.offs, bp.gids, 3 * np.pi ** 2 * JW * exact)
+    return m, bp, r, exact
+
+
+def test_reference_mode_known_answer():
+    """The reference's own correctness check (nekBone/main.cpp:105-131) on its
+    BP5 case, N=7, E=16x16x32=8192, tol 1e-6: the published run reports
+    maxError 1.02763e-07 in 78 iterations (nekBone/readme.md:39).  The oracle
+    (solve() with BPZeroMean on r and x, nekBone/main.cpp:24-31) must take the
+    same number of iterations and land within 3 % of that error."""
+    m, bp, r, exact = _reference_mode_problem(16, 16, 32)
+    L = m.E * m.Np
+    O.zero_mean(r, L)
+    x = np.zeros(L)
+    it = bp.pcg(r, x, 1e-6, 1000, precond=0)
+    O.zero_mean(x, L)
+    err = np.abs(exact - x).max()
+    assert it == 78
+    assert abs(err - 1.02763e-07) <= 0.03 * 1.02763e-07
+
+
+def test_zero_mean_restatement():
+    q = O.uniform(3 * 40, 9, 1, -1, 1)
+    q0 = q.copy()
+    O.zero_mean(q, 30, Nfields=3, offset=40)  # 30 local nodes per field, stride 40
+    mean = sum(q0[f * 40:f * 40 + 30].sum() for f in range(3)) / 90
+    assert np.allclose(q, q0 - mean, rtol=0, atol=1e-15)

@@ -184,3 +184,63 @@ def test_weighted_inner_products(nb, O, dev):
     assert abs(g1 - ref_ab) <= 1e-12 * abs(ref_ab) and abs(g2 - ref_aa) <= 1e-12 * ref_aa
     # deterministic: repeated calls give identical bits
     assert bp.weighted_inner_product(w, a, b) == got
+
+
+def _reference_mode(nb, dev, nx, ny, nz):
+    bp = nb.BP(7, nx, ny, nz, periodic=True, dirichlet=False, perturb=0.0, box=(-1.0, 1.0))
+    L = bp.Nlocal
+    X, Y, Z = (bp.device_array(c, L, torch.float64) for c in "xyz")
+    JW = bp.device_array("ggeo", 7 * L, torch.float64).view(bp.E, 7, bp.Np)[:, 0, :].reshape(-1)
+    exact = torch.cos(np.pi * X) * torch.cos(np.pi * Y) * torch.cos(np.pi * Z)
+    r = (3 * np.pi ** 2) * JW * exact
+    bp.ogs.gather_scatter_many(r)
+    return bp, r, exact
+
+
+def test_reference_mode_matches_oracle(nb, O, dev):
+    """BP5 reference mode (periodic [-1,1]^3, BK, COPY, zero mean) on 4x4x8
+    elements: after 60 fixed iterations the solution agrees with the oracle's
+    to 1e-10; to tol 1e-6 the iteration counts agree within one (the test
+    rdotr <= TOL can fall either side of the last iteration in rounding)."""
+    bp, r0, exact = _reference_mode(nb, dev, 4, 4, 8)
+    m = O.BoxMesh(7, 4, 4, 8, perturb=0.0, periodic=True, dirichlet=False, box=(-1.0, 1.0))
+    L = m.E * m.Np
+    JW = m.ggeo.reshape(m.E, 7, m.Np)[:, 0, :].reshape(-1)
+    ex = np.cos(np.pi * m.x) * np.cos(np.pi * m.y) * np.cos(np.pi * m.z)
+    obp = O.BP(m, np.concatenate([np.ones(L), np.zeros(L)]), bk=True)
+    f = O.gs_many_add(obp.Ng, obp.offs, obp.gids, 3 * np.pi ** 2 * JW * ex)
+    kw = dict(precond=nb.PRECOND_COPY, bk=True, zero_mean=True)
+    for tol, maxit, fixed in ((0.0, 60, True), (1e-6, 1000, False)):
+        r, x = r0.clone(), torch.zeros_like(r0)
+        st = bp.pcg(None, r, x, tol, maxit, fixed_iterations=fixed, **kw)
+        ro, xo = O.zero_mean(f.copy(), L), np.zeros(L)
+        it = obp.pcg(ro, xo, tol, maxit, precond=0, fixed=fixed)
+        O.zero_mean(xo, L)
+        assert st["status"] == 0
+        if fixed:
+            assert st["iterations"] == it == 60
+            assert np.abs(x.cpu().numpy() - xo).max() <= 1e-10 * np.abs(xo).max()
+        else:
+            assert abs(st["iterations"] - it) <= 1
+
+
+def test_reference_mode_known_answer(nb, dev):
+    """The reference's own correctness check on its BP5 case (N=7, E=8192,
+    tol 1e-6): published maxError 1.02763e-07 in 78 iterations
+    (nekBone/readme.md:39)."""
+    bp, r, exact = _reference_mode(nb, dev, 16, 16, 32)
+    x = torch.zeros_like(r)
+    st = bp.pcg(None, r, x, 1e-6, 1000, precond=nb.PRECOND_COPY, bk=True, zero_mean=True)
+    err = float((x - exact).abs().max())
+    assert st["status"] == 0 and st["iterations"] == 78
+    assert abs(err - 1.02763e-07) <= 0.03 * 1.02763e-07
+
+
+def test_zero_mean_entry(nb, O, dev):
+    bp = nb.BP(3, 2, 2, 2, Nfields=3, periodic=True, dirichlet=False)
+    q0 = O.uniform(3 * bp.offset, 12, 1, -1, 1)
+    q = torch.from_numpy(q0).to(dev)
+    bp.zero_mean(q)
+    torch.cuda.synchronize()
+    want = O.zero_mean(q0.copy(), bp.Nlocal, Nfields=3, offset=bp.offset)
+    assert np.abs(q.cpu().numpy() - want).max() <= 1e-14
