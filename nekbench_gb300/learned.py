@@ -3,7 +3,8 @@
 Data: residuals that the plain Jacobi-PCG itself produces, paired with a
 correction.  For each seeded problem (lambda0 = 1, lambda1 = 1 + 0.5
 sin(2 pi k.x) with k ~ U{1..4}^3, f ~ U[-1,1] assembled), the FP32 Jacobi-PCG
-iterate x_k after k iterations (k in SNAPSHOTS) gives the residual
+iterate x_k after k iterations (k spread over the whole solve: SNAPSHOT_FRACTIONS
+of its iteration count) gives the residual
 r_k = b - A x_k (FP64).  The default correction is the element-local block
 solve of r_k (exact on each element's interior nodes, Jacobi on its boundary),
 a fixed linear map of the element's own residual that a local network can
@@ -29,6 +30,20 @@ import numpy as np
 import nekbench_gb300 as nb
 
 SNAPSHOTS = (0, 10, 40, 120)
+# residual snapshots spread over a whole Jacobi-PCG solve (fractions of its
+# iteration count): late residuals are smooth across elements and must be in
+# the training set too
+SNAPSHOT_FRACTIONS = (0.0, 0.02, 0.08, 0.2, 0.35, 0.5, 0.65, 0.8, 0.95)
+
+
+def snapshot_schedule(bp, lam, f, torch, dev, fractions=SNAPSHOT_FRACTIONS):
+    """Iteration numbers at the given fractions of the Jacobi-PCG iteration
+    count (to relative residual 1e-8) of this problem."""
+    r = f.clone()
+    x = torch.zeros_like(f)
+    st = bp.pcg(lam, r, x, 1e-8, 20000, solver=nb.SOLVER_MIXED)
+    n = max(int(st["iterations"]), 1)
+    return sorted({int(round(q * n)) for q in fractions})
 
 
 def coefficients(bp, seed, torch):
@@ -49,7 +64,7 @@ def rhs(bp, seed, torch, dev):
     return f
 
 
-def generate_pairs(bp, seeds, torch, dev, frac=0.125, snapshots=SNAPSHOTS, horizon=16, log=None,
+def generate_pairs(bp, seeds, torch, dev, frac=0.125, snapshots=None, horizon=16, log=None,
                    target="local"):
     """Training pairs (inp, target), float32 device tensors of shape [M, Np].
 
@@ -74,13 +89,14 @@ def generate_pairs(bp, seeds, torch, dev, frac=0.125, snapshots=SNAPSHOTS, horiz
     for s in seeds:
         lam = coefficients(bp, s, torch)
         f = rhs(bp, s, torch, dev)
+        snaps = snapshots if snapshots is not None else snapshot_schedule(bp, lam, f, torch, dev)
         if horizon <= 0:
             r.copy_(f)
             xs.zero_()
             bp.pcg(lam, r, xs, 1e-9, 20000, solver=nb.SOLVER_MIXED)  # converged reference
         inv_diag = None
         rng = np.random.default_rng(10_000 + s)
-        for k in snapshots:
+        for k in snaps:
             if horizon > 0 and target == "pcg":
                 r.copy_(f)
                 xs.zero_()
