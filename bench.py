@@ -312,6 +312,7 @@ def pcg_comparison(nb, torch, dev, n, learned):
                        f"relative residual 1e-8", "E": bp.E, "unknowns_local": L}
     runs = [("fp64_jacobi", dict(solver=nb.SOLVER_FP64)),
             ("mixed_fp32_trilinear", dict(solver=nb.SOLVER_MIXED, inner_precision=nb.FP32_TRILINEAR)),
+            ("mixed_fp32", dict(solver=nb.SOLVER_MIXED, inner_precision=nb.FP32)),
             ("mixed_bf16", dict(solver=nb.SOLVER_MIXED, inner_precision=nb.BF16))]
     net = None
     if learned:

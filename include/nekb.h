@@ -218,6 +218,12 @@ typedef struct {
   int zero_mean;        /* 1: nekb_bp_zero_mean on r before and on x after the
                            solve, as solve() does for an all-Neumann problem
                            (nekBone/main.cpp:24-31)                             */
+  int fcg_window;       /* learned preconditioner: the new direction is made
+                           A-orthogonal to the last fcg_window directions
+                           (truncated flexible CG, FCG(m), 1..8; 0: 5).  A
+                           nonlinear preconditioner needs m > 1: with m = 1
+                           (the reference's flexible beta, solve.cpp:92-95)
+                           conjugacy is lost over long solves              */
 } nekb_pcg_opts;
 
 typedef struct {

@@ -67,7 +67,8 @@ class PcgOpts(C.Structure):
     _fields_ = [("solver", C.c_int), ("precond", C.c_int), ("flexible", C.c_int),
                 ("fixed_iterations", C.c_int), ("bk", C.c_int), ("inner_precision", C.c_int),
                 ("inner_tol", C.c_double), ("max_outer", C.c_int), ("check_every", C.c_int),
-                ("use_graph", C.c_int), ("net", C.c_void_p), ("zero_mean", C.c_int)]
+                ("use_graph", C.c_int), ("net", C.c_void_p), ("zero_mean", C.c_int),
+                ("fcg_window", C.c_int)]
 
 
 class PcgStats(C.Structure):
@@ -436,7 +437,7 @@ class BP:
     def pcg(self, lam, r, x, tol, maxit, solver=SOLVER_FP64, precond=PRECOND_JACOBI,
             flexible=False, fixed_iterations=False, bk=False, inner_precision=FP32_TRILINEAR,
             inner_tol=1e-2, max_outer=40, check_every=16, use_graph=True, net=None,
-            zero_mean=False):
+            zero_mean=False, fcg_window=0):
         """BPPCG: r (rhs in, residual out) and x (guess in, solution out) are device FP64;
         zero_mean: BPZeroMean on r before and on x after, as solve() does for an
         all-Neumann problem."""
@@ -448,6 +449,7 @@ class BP:
         o.check_every, o.use_graph = check_every, int(use_graph)
         o.net = net.h if net is not None else None
         o.zero_mean = int(zero_mean)
+        o.fcg_window = int(fcg_window)
         st = PcgStats()
         _order_after_torch()
         check(lib().nekb_bp_pcg(self.h, _ptr(lam), _ptr(r), _ptr(x), tol, maxit, C.byref(o),

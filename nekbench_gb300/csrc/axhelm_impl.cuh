@@ -241,6 +241,7 @@ k_axhelm(const AxArgs a)
   }
   __syncthreads();
 
+  T qaq = T(0);  // this thread's share of q . Aq (when asked for)
   if (active) {
     T* Aqe = static_cast<T*>(a.Aq) + element * NP + ij;
 #pragma unroll
@@ -275,7 +276,22 @@ k_axhelm(const AxArgs a)
         T out = ar + as + at;
         if (!BK) out += wl1 * r_q[f][k];
         Aqe[f * a.offset + k * NQ2] = out;
+        qaq += r_q[f][k] * out;
       }
+    }
+  }
+  if (!PARTIAL && a.dot_partials != nullptr) {  // block sum in a fixed order
+    __shared__ double s_red[32];
+    double v = (double)qaq;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((tid & 31) == 0) s_red[tid >> 5] = v;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_red[w];
+      a.dot_partials[blockIdx.x] = t;
+      if (blockIdx.x == 0) *a.dot_count = (int)gridDim.x;
     }
   }
 }

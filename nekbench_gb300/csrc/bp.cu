@@ -35,9 +35,12 @@ DeviceBuf::~DeviceBuf()
   if (p) cudaFree(p);
 }
 
-int apply_op(const OpView& op, const void* q, void* Aq, const int* skip, cudaStream_t s)
+int apply_op(const OpView& op, const void* q, void* Aq, const int* skip, cudaStream_t s,
+             double* dot_partials, int* dot_count)
 {
   AxArgs a{};
+  a.dot_partials = dot_partials;
+  a.dot_count = dot_count;
   a.Nelements = op.E;
   a.offset = op.offset;
   a.elementList = nullptr;

@@ -27,12 +27,23 @@ struct OpView {
   float w1d[kMaxNq] = {};
 };
 
-int apply_op(const OpView& op, const void* q, void* Aq, const int* skip, cudaStream_t s);
+// Aq = mask(gs(axhelm(q))); with dot_partials, the operator kernel also leaves
+// per-block sums of q . axhelm(q) (before assembly) and their count
+int apply_op(const OpView& op, const void* q, void* Aq, const int* skip, cudaStream_t s,
+             double* dot_partials = nullptr, int* dot_count = nullptr);
+
+// longest window of truncated flexible CG, FCG(m)
+constexpr int kFcgMax = 8;
 
 // device state of one PCG run; updated by the last block of each reduction
 struct PcgState {
   double rdotz1, rdotz2, rdotr, rdotr0, TOL, alpha, beta, pAp, tol2, zdotAp;
   int iter, done, result, status, maxit, flexible, fixed, pad;
+  // FCG(m): z . A p_j of the current z and p_j . A p_j for the kept
+  // directions (ring slots), the window m, the directions kept and the slot
+  // the next direction goes to
+  double fcg_zap[kFcgMax], fcg_pap[kFcgMax];
+  int fcg_m, fcg_count, fcg_head, fcg_pad;
 };
 
 struct DeviceBuf {
@@ -60,6 +71,10 @@ struct nekb_bp {
   nekb::DeviceBuf p, z, Ap, Ax, invDiag, b, rr;
   // FP32 workspace of the inner solver
   nekb::DeviceBuf r32, x32, p32, z32, Ap32, invDiag32, lam32;
+  // FCG(m) directions p_j and A p_j (kFcgMax slots of Nfields*offset floats each)
+  nekb::DeviceBuf fcgP, fcgAP;
+  // per-block p . A p sums of the FP32 operator (one per operator block) + count
+  nekb::DeviceBuf axdot;
   // reduction scratch and solver state
   nekb::DeviceBuf partials, counter, state;
   nekb::PcgState* h_state = nullptr;  // pinned mirror

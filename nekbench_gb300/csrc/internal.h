@@ -61,6 +61,10 @@ struct AxArgs {
   const void* q;
   void* Aq;
   const int* skip;      // optional device flag: kernel returns at once when *skip != 0
+  // optional: per-block sums of q . Aq (local, before assembly) into
+  // dot_partials[block], the block count into *dot_count (non-Partial forms)
+  double* dot_partials;
+  int* dot_count;
   float r1d[kMaxNq];    // GLL nodes and weights (trilinear geometry only)
   float w1d[kMaxNq];
 };

@@ -281,6 +281,168 @@ __global__ void __launch_bounds__(RT) k_pupdate(PcgArgs<T> a)
   }
 }
 
+// ---- truncated flexible CG, FCG(m), for the external (learned) preconditioner.
+// The last m directions p_j and A p_j sit in ring slots (stride `ring`
+// entries); the new direction is z minus its A-projections on them,
+//   p = z - sum_j (z . A p_j / p_j . A p_j) p_j ,  alpha = r . p / p . A p .
+
+// (r, z) sums and z . A p_j for the kept directions; REFRESH: same iteration
+template <typename T, int V, bool REFRESH>
+__global__ void __launch_bounds__(RT) k_fcg_dots(PcgArgs<T> a, const T* __restrict__ AP, int64_t ring)
+{
+  PcgState* st = a.st;
+  if (st->done) return;
+  const int cnt = st->fcg_count;
+  T rz = 0, rr = 0, zap[kFcgMax];
+#pragma unroll
+  for (int j = 0; j < kFcgMax; ++j) zap[j] = 0;
+  const int64_t stride = (int64_t)gridDim.x * RT;
+  const int64_t nv = a.Nloc / V;
+  for (int f = 0; f < a.NF; ++f) {
+    const int64_t fo = f * a.offset;
+    for (int64_t iv = (int64_t)blockIdx.x * RT + threadIdx.x; iv < nv; iv += stride) {
+      const int64_t i = iv * V, n = i + fo;
+      T r[V], z[V], w[V];
+      vld<V>(a.r + n, r);
+      vld<V>(a.z + n, z);
+      vld<V>(a.w + i, w);
+#pragma unroll
+      for (int l = 0; l < V; ++l) {
+        rz += w[l] * r[l] * z[l];
+        rr += w[l] * r[l] * r[l];
+      }
+#pragma unroll
+      for (int j = 0; j < kFcgMax; ++j) {
+        if (j < cnt) {
+          T ap[V];
+          vld<V>(AP + j * ring + n, ap);
+#pragma unroll
+          for (int l = 0; l < V; ++l) zap[j] += w[l] * z[l] * ap[l];
+        }
+      }
+    }
+  }
+  double v[2 + kFcgMax];
+  v[0] = (double)rz;
+  v[1] = (double)rr;
+#pragma unroll
+  for (int j = 0; j < kFcgMax; ++j) v[2 + j] = (double)zap[j];
+  if (grid_sum<2 + kFcgMax>(v, a.partials, a.counter)) {
+    if (REFRESH)
+      state_refresh(st, v[0], v[1], 0.0);
+    else
+      state_after_rz(st, v[0], v[1], 0.0);
+#pragma unroll
+    for (int j = 0; j < kFcgMax; ++j) st->fcg_zap[j] = v[2 + j];
+  }
+}
+
+// p = z - sum_j c_j p_j into the operator's p and into the ring slot `head`
+template <typename T, int V>
+__global__ void __launch_bounds__(RT) k_fcg_pupdate(PcgArgs<T> a, T* __restrict__ P, int64_t ring)
+{
+  const PcgState* st = a.st;
+  if (st->done) return;
+  const int cnt = st->fcg_count, head = st->fcg_head;
+  T c[kFcgMax];
+#pragma unroll
+  for (int j = 0; j < kFcgMax; ++j)
+    c[j] = (j < cnt && st->fcg_pap[j] > 0.0) ? (T)(st->fcg_zap[j] / st->fcg_pap[j]) : T(0);
+  const int64_t N = a.NF * a.offset / V;
+  for (int64_t nv = (int64_t)blockIdx.x * RT + threadIdx.x; nv < N; nv += (int64_t)gridDim.x * RT) {
+    T p[V];
+    vld<V>(a.z + nv * V, p);
+#pragma unroll
+    for (int j = 0; j < kFcgMax; ++j) {
+      if (j < cnt) {
+        T pj[V];
+        vld<V>(P + j * ring + nv * V, pj);
+#pragma unroll
+        for (int l = 0; l < V; ++l) p[l] -= c[j] * pj[l];
+      }
+    }
+    vst<V>(a.p + nv * V, p);
+    vst<V>(P + head * ring + nv * V, p);
+  }
+}
+
+// pAp = sum w p Ap, rp = sum w r p; alpha = rp / pAp; A p into the ring slot;
+// the slot becomes a kept direction
+template <typename T, int V>
+__global__ void __launch_bounds__(RT) k_fcg_pap(PcgArgs<T> a, T* __restrict__ AP, int64_t ring)
+{
+  PcgState* st = a.st;
+  if (st->done) return;
+  const int head = st->fcg_head;
+  T pap = 0, rp = 0;
+  const int64_t stride = (int64_t)gridDim.x * RT;
+  const int64_t nv = a.Nloc / V;
+  for (int f = 0; f < a.NF; ++f) {
+    const int64_t fo = f * a.offset;
+    for (int64_t iv = (int64_t)blockIdx.x * RT + threadIdx.x; iv < nv; iv += stride) {
+      const int64_t i = iv * V, n = i + fo;
+      T w[V], p[V], ap[V], r[V];
+      vld<V>(a.w + i, w);
+      vld<V>(a.p + n, p);
+      vld<V>(a.Ap + n, ap);
+      vld<V>(a.r + n, r);
+      vst<V>(AP + head * ring + n, ap);
+#pragma unroll
+      for (int l = 0; l < V; ++l) {
+        pap += w[l] * p[l] * ap[l];
+        rp += w[l] * r[l] * p[l];
+      }
+    }
+  }
+  double v[2] = {(double)pap, (double)rp};
+  if (grid_sum<2>(v, a.partials, a.counter)) {
+    const double pAp = v[0], alpha = v[1] / pAp;
+    st->pAp = pAp;
+    if (!(pAp > 0.0) || !isfinite(alpha)) {
+      st->done = 1;
+      st->result = st->iter - 1;
+      st->status = NEKB_ERR_BREAKDOWN;
+      return;
+    }
+    st->alpha = alpha;
+    st->fcg_pap[head] = pAp;
+    st->fcg_head = (head + 1) % st->fcg_m;
+    st->fcg_count = st->fcg_count < st->fcg_m ? st->fcg_count + 1 : st->fcg_m;
+  }
+}
+
+// pAp from the operator's per-block sums of p . (A p)_local.  For a p that is
+// continuous across element copies and zero on masked nodes, the
+// invDegree-weighted sum of p . mask(gs(A_local p)) equals the plain sum of
+// p . A_local p over all local nodes, so the operator kernel can form it in
+// its epilogue and no pass over p and Ap is needed; alpha = rdotz / pAp.
+__global__ void __launch_bounds__(1024) k_pap_partials(PcgState* st, const double* __restrict__ part,
+                                                       const int* __restrict__ count)
+{
+  if (st->done) return;
+  __shared__ double sh[32];
+  const int n = *count;
+  double v = 0.0;
+  for (int b = threadIdx.x; b < n; b += blockDim.x) v += part[b];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double pAp = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) pAp += sh[w];
+    const double alpha = st->rdotz1 / pAp;
+    st->pAp = pAp;
+    if (!(pAp > 0.0) || !isfinite(alpha)) {
+      st->done = 1;
+      st->result = st->iter - 1;
+      st->status = NEKB_ERR_BREAKDOWN;
+      return;
+    }
+    st->alpha = alpha;
+  }
+}
+
 // pAp = sum w p Ap ; alpha = rdotz / pAp
 template <typename T, int V = 1>
 __global__ void __launch_bounds__(RT) k_pap(PcgArgs<T> a)
@@ -406,12 +568,6 @@ __global__ void k_mask_set(int64_t Nm, const int32_t* ids, double v, double* q)
     q[ids[n]] = v;
 }
 
-__global__ void k_d2f_scaled(int64_t N, const double* a, float* b)
-{
-  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x)
-    b[n] = (float)a[n];
-}
-
 inline unsigned red_grid(int64_t n)
 {
   int64_t b = (n + RT - 1) / RT;
@@ -428,13 +584,36 @@ inline unsigned vec_grid(int64_t n)
   return (unsigned)b;
 }
 
-// the external (learned) preconditioner: z = M(r), launched on the stream
+// the external (learned) preconditioner: z = M(r), launched on the stream;
+// with m > 1 the iteration is FCG(m) on the ring buffers P, AP
 struct ExtPrecond {
   nekb_bp* bp = nullptr;
   nekb_net* net = nullptr;
   const float* invDiag = nullptr;
   const float* w = nullptr;
+  int m = 1;
+  float* P = nullptr;
+  float* AP = nullptr;
+  // FP32 operator with the pAp sums fused into its epilogue (null: separate pass)
+  double* axdot = nullptr;
+  int* axdot_count = nullptr;
 };
+
+template <typename T, bool REFRESH>
+int launch_fcg_dots(const PcgArgs<T>& a, const ExtPrecond* ext, cudaStream_t s)
+{
+  if constexpr (sizeof(T) == 4) {
+    const int64_t ring = a.NF * a.offset;
+    if (a.Nloc % 4 == 0 && a.offset % 4 == 0)
+      k_fcg_dots<T, 4, REFRESH><<<red_grid(a.Nloc / 4), RT, 0, s>>>(a, ext->AP, ring);
+    else
+      k_fcg_dots<T, 1, REFRESH><<<red_grid(a.Nloc), RT, 0, s>>>(a, ext->AP, ring);
+    NEKB_CUDA(cudaGetLastError());
+    return NEKB_OK;
+  } else {
+    return fail(NEKB_ERR_UNSUPPORTED, "FCG(m) runs in FP32 only");
+  }
+}
 
 // float4 access when the vectors allow it (FP32, lengths and offsets multiples of 4)
 template <typename T>
@@ -474,10 +653,40 @@ int launch_rz(const PcgArgs<T>& a, int mode, bool flex, cudaStream_t s)
   return NEKB_OK;
 }
 
+// one FCG(m) iteration with the external preconditioner (FP32)
+template <typename T>
+int launch_fcg_iteration(const OpView& op, PcgArgs<T> a, const ExtPrecond* ext, cudaStream_t s)
+{
+  if constexpr (sizeof(T) == 4) {
+    const int64_t Nall = a.NF * a.offset;
+    const bool v4 = vec_width(a) == 4;
+    if (v4) {
+      k_fcg_pupdate<T, 4><<<vec_grid(Nall / 4), RT, 0, s>>>(a, ext->P, Nall);
+    } else {
+      k_fcg_pupdate<T, 1><<<vec_grid(Nall), RT, 0, s>>>(a, ext->P, Nall);
+    }
+    NEKB_CUDA(cudaGetLastError());
+    NEKB_TRY(apply_op(op, a.p, a.Ap, &a.st->done, s));
+    if (v4) {
+      k_fcg_pap<T, 4><<<red_grid(a.Nloc / 4), RT, 0, s>>>(a, ext->AP, Nall);
+    } else {
+      k_fcg_pap<T, 1><<<red_grid(a.Nloc), RT, 0, s>>>(a, ext->AP, Nall);
+    }
+    NEKB_CUDA(cudaGetLastError());
+    k_update<T><<<vec_grid(Nall), RT, 0, s>>>(a);
+    NEKB_CUDA(cudaGetLastError());
+    NEKB_TRY(net_precondition(ext->bp, ext->net, a.r, a.z, ext->invDiag, ext->w, &a.st->done, s));
+    return launch_fcg_dots<T, false>(a, ext, s);
+  } else {
+    return fail(NEKB_ERR_UNSUPPORTED, "FCG(m) runs in FP32 only");
+  }
+}
+
 template <typename T>
 int launch_iteration(const OpView& op, PcgArgs<T> a, int mode, bool flex, const ExtPrecond* ext,
                      cudaStream_t s)
 {
+  if (mode == PC_EXTERNAL && ext && ext->m > 1) return launch_fcg_iteration<T>(op, a, ext, s);
   const int64_t Nall = a.NF * a.offset;
   const int V = vec_width(a);
   const unsigned vg = vec_grid(Nall / V), rg = red_grid(a.Nloc / V);
@@ -496,11 +705,17 @@ int launch_iteration(const OpView& op, PcgArgs<T> a, int mode, bool flex, const 
       k_pupdate<T, PC_JACOBI, 1><<<vg, RT, 0, s>>>(a);
   }
   NEKB_CUDA(cudaGetLastError());
-  NEKB_TRY(apply_op(op, a.p, a.Ap, &a.st->done, s));
-  if constexpr (sizeof(T) == 4) {
-    if (V == 4) k_pap<T, 4><<<rg, RT, 0, s>>>(a);
+  if (sizeof(T) == 4 && ext && ext->axdot) {
+    // FP32 operator: pAp from the operator kernel's own partial sums
+    NEKB_TRY(apply_op(op, a.p, a.Ap, &a.st->done, s, ext->axdot, ext->axdot_count));
+    k_pap_partials<<<1, 1024, 0, s>>>(a.st, ext->axdot, ext->axdot_count);
+  } else {
+    NEKB_TRY(apply_op(op, a.p, a.Ap, &a.st->done, s));
+    if constexpr (sizeof(T) == 4) {
+      if (V == 4) k_pap<T, 4><<<rg, RT, 0, s>>>(a);
+    }
+    if (V == 1) k_pap<T, 1><<<rg, RT, 0, s>>>(a);
   }
-  if (V == 1) k_pap<T, 1><<<rg, RT, 0, s>>>(a);
   NEKB_CUDA(cudaGetLastError());
   if (mode == PC_EXTERNAL) {
     k_update<T><<<vec_grid(Nall), RT, 0, s>>>(a);
@@ -522,6 +737,7 @@ int launch_first_rz(PcgArgs<T> a, int mode, bool flex, const ExtPrecond* ext, cu
     if constexpr (sizeof(T) == 4) {
       NEKB_TRY(net_precondition(ext->bp, ext->net, a.r, a.z, ext->invDiag, ext->w, &a.st->done, s));
     }
+    if (ext->m > 1) return launch_fcg_dots<T, false>(a, ext, s);
   }
   return launch_rz<T, false, false>(a, mode, flex, s);
 }
@@ -553,6 +769,7 @@ int launch_refresh_rz(PcgArgs<T> a, int mode, bool flex, const ExtPrecond* ext, 
     if constexpr (sizeof(T) == 4) {
       NEKB_TRY(net_precondition(ext->bp, ext->net, a.r, a.z, ext->invDiag, ext->w, &a.st->done, s));
     }
+    if (ext->m > 1) return launch_fcg_dots<T, true>(a, ext, s);
   }
   return launch_rz<T, false, true>(a, mode, flex, s);
 }
@@ -589,6 +806,9 @@ int pcg_core(nekb_bp* bp, const OpView& op, T* r, T* x, const T* w, const T* inv
   h.maxit = maxit;
   h.flexible = flex ? 1 : 0;
   h.fixed = fixed ? 1 : 0;
+  h.fcg_m = (mode == PC_EXTERNAL && ext && ext->m > 1) ? ext->m : 1;
+  h.fcg_count = 0;
+  h.fcg_head = 0;
   PcgState* st = bp->state.as<PcgState>();
   *bp->h_state = h;
   NEKB_CUDA(cudaMemcpyAsync(st, bp->h_state, sizeof(PcgState), cudaMemcpyHostToDevice, s));
@@ -614,7 +834,7 @@ int pcg_core(nekb_bp* bp, const OpView& op, T* r, T* x, const T* w, const T* inv
   if (use_graph) {
     auto key = std::make_tuple(op.precision * 64 + mode * 4 + (flex ? 2 : 0) + (int)(sizeof(T) == 8),
                                chunk, op.flags, (const void*)op.lambda, (const void*)r, (const void*)x,
-                               (int)(ext && ext->net ? 1 : 0));
+                               (int)(ext && ext->net ? 1 + ext->m : 0));
     auto it = bp->graphs.find(key);
     if (it != bp->graphs.end()) {
       gexec = it->second;
@@ -849,6 +1069,23 @@ int solve_mixed(nekb_bp* bp, const double* lambda, double* r, double* x, double 
   ext.net = (nekb_net*)o.net;
   ext.invDiag = bp->invDiag32.as<float>();
   ext.w = bp->invdeg_f.as<float>();
+  {
+    // one partial per operator block: at most one block per element
+    NEKB_TRY(bp->axdot.ensure(sizeof(double) * (bp->E + 8)));
+    ext.axdot = bp->axdot.as<double>() + 8;
+    ext.axdot_count = reinterpret_cast<int*>(bp->axdot.as<double>());
+  }
+  if (learned) {
+    ext.m = o.fcg_window > 0 ? o.fcg_window : 5;
+    if (ext.m > kFcgMax) return fail(NEKB_ERR_INVALID, "fcg_window %d > %d", o.fcg_window, kFcgMax);
+    if (ext.m > 1) {
+      // sized for the longest window once, so captured graphs keep valid pointers
+      NEKB_TRY(bp->fcgP.ensure(sizeof(float) * kFcgMax * Nall));
+      NEKB_TRY(bp->fcgAP.ensure(sizeof(float) * kFcgMax * Nall));
+      ext.P = bp->fcgP.as<float>();
+      ext.AP = bp->fcgAP.as<float>();
+    }
+  }
   const int mode = learned ? PC_EXTERNAL : (jacobi ? PC_JACOBI : PC_COPY);
   const bool flex = learned || o.flexible != 0;
   if (rdotr > TOL) {
@@ -921,6 +1158,8 @@ int solve_mixed(nekb_bp* bp, const double* lambda, double* r, double* x, double 
         hs.rdotz2 = 0.0;
         hs.alpha = 0.0;
         hs.beta = 0.0;
+        hs.fcg_count = 0;
+        hs.fcg_head = 0;
         NEKB_CUDA(cudaMemsetAsync(a.p, 0, sizeof(float) * Nall, s));
         NEKB_CUDA(cudaMemsetAsync(a.Ap, 0, sizeof(float) * Nall, s));
         NEKB_CUDA(cudaMemcpyAsync(a.st, &hs, sizeof(PcgState), cudaMemcpyHostToDevice, s));

@@ -17,7 +17,11 @@ removed).
 
 Training runs the network's own fused forward/backward kernels and Adam
 (nekb_net_train_step); evaluation compares flexible PCG with the network
-against Jacobi-PCG to the same true FP64 relative residual.  torch only holds
+against Jacobi-PCG to the same true FP64 relative residual.  The network is
+nonlinear, so the flexible iteration keeps several directions (FCG(m), m = 5
+by default): with the single-direction flexible beta the Krylov space loses
+conjugacy over a long solve and the network costs iterations instead of
+saving them.  torch only holds
 device buffers and gathers element subsets.
 """
 from __future__ import annotations
@@ -152,7 +156,8 @@ def train(net, inp, tgt, torch, steps=2000, batch=2048, lr=1e-3, seed=0, log=Non
     return losses
 
 
-def evaluate(bp, net, seeds, torch, dev, tol=1e-8, inner_precision=None, solver=None):
+def evaluate(bp, net, seeds, torch, dev, tol=1e-8, inner_precision=None, solver=None,
+             fcg_window=0):
     """Iterations and time to `tol` (true FP64 relative residual) with and without
     the network, on the same problems."""
     inner_precision = nb.FP32_TRILINEAR if inner_precision is None else inner_precision
@@ -165,7 +170,8 @@ def evaluate(bp, net, seeds, torch, dev, tol=1e-8, inner_precision=None, solver=
         f = rhs(bp, s, torch, dev)
         row = {"seed": int(s)}
         maxit = 20000
-        for name, kw in (("jacobi", {}), ("learned", {"precond": nb.PRECOND_LEARNED, "net": net})):
+        for name, kw in (("jacobi", {}), ("learned", {"precond": nb.PRECOND_LEARNED, "net": net,
+                                                      "fcg_window": fcg_window})):
             best = None
             for _ in range(2):
                 r.copy_(f)

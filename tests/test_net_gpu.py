@@ -177,3 +177,30 @@ def test_inference_mode_falls_back_where_not_built(nb):
     assert net.inference == nb.NET_FP32
     with pytest.raises(nb.NekbError):
         net.inference = 7
+
+
+def test_fcg_window_with_a_zero_network_matches_jacobi(nb, O, dev):
+    """A network whose last layer is zero adds nothing to Jacobi: FCG(m) for
+    m = 1, 5, 8 (ring of kept directions, fused projections) is then PCG with
+    Jacobi in exact arithmetic, so it takes the Jacobi-PCG count within a few
+    iterations and reaches the FP64 tolerance; m = 9 is refused."""
+    bp = nb.BP(7, 4, 4, 4, perturb=0.1, seed=3)
+    L = bp.Nlocal
+    lam = torch.cat([torch.full((L,), 1.0), torch.full((L,), 1.5)]).double().to(dev)
+    f = torch.from_numpy(O.uniform(L, 8, 3, -1, 1)).to(dev)
+    bp.ogs.gather_scatter_many(f)
+    r, x = f.clone(), torch.zeros_like(f)
+    jac = bp.pcg(lam, r, x, 1e-8, 2000, solver=nb.SOLVER_MIXED)
+    net = nb.Net(8, 16, 3, seed=11)
+    W = net.weights()
+    W[27 * 16 + 27 * 16 * 16:] = 0.0
+    net.set_weights(W)
+    for m in (1, 5, 8):
+        r, x = f.clone(), torch.zeros_like(f)
+        st = bp.pcg(lam, r, x, 1e-8, 2000, solver=nb.SOLVER_MIXED, precond=nb.PRECOND_LEARNED,
+                    net=net, fcg_window=m)
+        assert st["status"] == 0 and st["true_rel_res"] <= 1e-8
+        assert abs(st["iterations"] - jac["iterations"]) <= 3, (m, st, jac)
+    with pytest.raises(nb.NekbError):
+        bp.pcg(lam, f.clone(), torch.zeros_like(f), 1e-8, 10, solver=nb.SOLVER_MIXED,
+               precond=nb.PRECOND_LEARNED, net=net, fcg_window=9)
