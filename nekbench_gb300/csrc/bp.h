@@ -81,7 +81,6 @@ struct nekb_bp {
   // CUDA graphs of one chunk of PCG iterations, keyed by their arguments
   std::map<std::tuple<int, int, int, const void*, const void*, const void*, int>, cudaGraphExec_t> graphs;
   void* net = nullptr;  // learned preconditioner in use (nekb_net*)
-  nekb::DeviceBuf net_tmp;
 };
 
 namespace nekb {

@@ -148,8 +148,11 @@ __device__ void load_weights(const TW* W, float* sW, int C)
   }
 }
 
-// normalize: input h r_e / s_e with h = sqrt(invDiag) per node (1 without
-// invDiag) and s_e = RMS of h r_e; output times w * h * s_e.  The symmetric
+// mode bit kNetNormalize: input h r_e / s_e with h = sqrt(invDiag) per node (1
+// without invDiag) and s_e = RMS of h r_e; output times w * h * s_e.  Bit
+// kNetAddJacobi: w * invDiag * r is added to the output, so that a gather-
+// scatter of it yields invDiag r + gs(w h s net) (invDiag and r are continuous
+// across element copies and the weights w of a group sum to one).  The symmetric
 // diagonal scaling makes the map the network has to represent nearly uniform
 // across the GLL nodes (whose weights span three decades at N=7) and
 // independent of the element size.
@@ -177,7 +180,7 @@ k_net_infer(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ Wbf,
     const float h = (act && invDiag) ? sqrtf(invDiag[(e % Efield) * NP + n]) : 1.f;
     const float v = act ? h * r[e * NP + n] : 0.f;
     float s = 1.f;
-    if (normalize) s = sqrtf(block_sum_f(v * v, red) / NP);
+    if (normalize & kNetNormalize) s = sqrtf(block_sum_f(v * v, red) / NP);
     const float inv = s > 0.f ? 1.f / s : 0.f;
     if (act) a0[n] = v * inv;
     __syncthreads();
@@ -199,7 +202,9 @@ k_net_infer(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ Wbf,
       float acc[1];
       conv_fwd<NQ, C, 1>(a2, sW + o3, n, msk, acc);
       const float wn = w ? w[(e % Efield) * NP + n] : 1.f;
-      out[e * NP + n] = wn * h * s * acc[0];
+      float o = h * s * acc[0];
+      if ((normalize & kNetAddJacobi) && invDiag) o += invDiag[(e % Efield) * NP + n] * r[e * NP + n];
+      out[e * NP + n] = wn * o;
     }
     __syncthreads();
   }
@@ -375,16 +380,6 @@ __global__ void k_to_bf16(int P, const float* W, __nv_bfloat16* Wbf)
 {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p < P) Wbf[p] = __float2bfloat16_rn(W[p]);
-}
-
-// z = zn + invDiag * r  (zn already gathered-scattered)
-__global__ void k_net_combine(int64_t N, int64_t Nloc, const float* __restrict__ zn,
-                              const float* __restrict__ invDiag, const float* __restrict__ r,
-                              float* __restrict__ z, const int* skip)
-{
-  if (skip != nullptr && *skip != 0) return;
-  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x)
-    z[n] = zn[n] + invDiag[n % Nloc] * r[n];
 }
 
 // in = h r_e / s_e ; target = (e_e - invDiag r_e) / (h s_e), h = sqrt(invDiag) per node
@@ -627,15 +622,11 @@ int net_precondition(nekb_bp* bp, nekb_net* net, const float* r, float* z, const
 {
   if (!net) return fail(NEKB_ERR_INVALID, "learned preconditioner: no network");
   if (net->Nq != bp->Nq) return fail(NEKB_ERR_INVALID, "net order Nq=%d differs from the mesh's %d", net->Nq, bp->Nq);
-  const int64_t Nall = bp->Nfields * bp->offset;
-  NEKB_TRY(bp->net_tmp.ensure(sizeof(float) * Nall));
-  float* tmp = bp->net_tmp.as<float>();
-  NEKB_TRY(net_infer(net, bp->Nfields * bp->E, bp->E, r, w, invDiag, tmp, 1, skip, s));
+  // z = w (h s net + invDiag r) per element copy, then assembled and masked
+  NEKB_TRY(net_infer(net, bp->Nfields * bp->E, bp->E, r, w, invDiag, z,
+                     kNetNormalize | kNetAddJacobi, skip, s));
   NEKB_TRY(launch_gs_add(bp->ogs->Nmulti, bp->ogs->d_offsets, bp->ogs->d_ids, bp->Nfields,
-                         bp->offset, tmp, NEKB_FLOAT, skip, s));
-  const unsigned g = (unsigned)std::min<int64_t>((Nall + 255) / 256, 152 * 16);
-  k_net_combine<<<g, 256, 0, s>>>(Nall, bp->offset, tmp, invDiag, r, z, skip);
-  NEKB_CUDA(cudaGetLastError());
+                         bp->offset, z, NEKB_FLOAT, skip, s));
   NEKB_TRY(launch_mask(bp->Nmasked, bp->mask.as<int32_t>(), bp->Nfields, bp->offset, z, NEKB_FLOAT,
                        skip, s));
   return NEKB_OK;

@@ -13,6 +13,10 @@ namespace nekb {
 int net_precondition(nekb_bp* bp, nekb_net* net, const float* r, float* z, const float* invDiag,
                      const float* w, const int* skip, cudaStream_t s);
 
+// inference mode bits: normalise by the element RMS of sqrt(invDiag) r; add
+// w invDiag r to the output
+constexpr int kNetNormalize = 1, kNetAddJacobi = 2;
+
 // tensor-core inference (nn_tc.cu): Nq=8, 16 channels
 bool net_tc_supported(int Nq, int C);
 int net_infer_tc(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const float* r,
