@@ -2,19 +2,17 @@
 // 512 nodes) and 16 channels: the three 3x3x3 convolutions of an element as
 // implicit GEMMs on the BF16 tensor cores (mma.m16n8k16, FP32 accumulation).
 //
-// One CTA of 8 warps per element at a time (persistent grid, two CTAs per
-// SM).  Node n = i + 8j + 64k; warp w owns the 16 nodes j in {2(w%4),
-// 2(w%4)+1}, i = 0..7 of every plane k (one m16 row tile per plane) and the
-// output channels 8(w/4) .. 8(w/4)+7, so each warp holds half of the weights
-// and accumulators.
+// One CTA of 4 warps per element at a time (persistent grid).  Node n =
+// i + 8j + 64k; warp w owns the 16 nodes j in {2w, 2w+1}, i = 0..7 of every
+// plane k (one m16 row tile per plane).
 //   layer 1 (1 -> 16):  A[node][tap] gathered from the scaled residual (27 taps
 //                        padded to K=32), B = W1[tap][co].
 //   layer 2 (16 -> 16): per tap a GEMM with K = 16 input channels.  The
 //                        activation tile of plane p shifted by (di,dj) is loaded
 //                        once (ldmatrix, out-of-element rows point to a zero
 //                        row) and multiplied into the accumulators of output
-//                        planes p+1, p, p-1 (taps dk = -1, 0, +1); the warp's 27
-//                        weight fragments stay in registers for the whole kernel.
+//                        planes p+1, p, p-1 (taps dk = -1, 0, +1); the 27 weight
+//                        fragments stay in registers for the whole kernel.
 //   layer 3 (16 -> 1):  U[node][tap] = act[node][:] . W3[:][tap] (N = 27 taps
 //                        padded to 32), then out[n] = sum_t U[n + off_t][t].
 // Activations are rounded to BF16 between layers (GELU outputs and the scaled
@@ -28,7 +26,7 @@
 namespace nekb {
 namespace {
 
-constexpr int kNq = 8, kNp = 512, kTaps = 27, kThreads = 256;
+constexpr int kNq = 8, kNp = 512, kTaps = 27, kThreads = 128;
 constexpr int kUStride = 516;  // floats; makes the fragment stores of U conflict-free
 constexpr int kO2 = kTaps * 16, kO3 = kTaps * 16 + kTaps * 16 * 16;
 
@@ -87,17 +85,14 @@ __device__ __forceinline__ uint32_t wpair(const uint16_t* W, int i0, int i1, boo
   return lo | (hi << 16);
 }
 
-__device__ __forceinline__ float block_sum8(float v, float* red)
+__device__ __forceinline__ float block_sum4(float v, float* red)
 {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   __syncthreads();
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
-  float s = 0.f;
-#pragma unroll
-  for (int w = 0; w < kThreads / 32; ++w) s += red[w];
-  return s;
+  return red[0] + red[1] + red[2] + red[3];
 }
 
 __global__ void __launch_bounds__(kThreads, 2)
@@ -115,46 +110,44 @@ k_net_infer_tc(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ W
   const uint32_t act_s = smem_addr(smem + kSmAct), zero_s = smem_addr(smem + kSmZero);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int g = lane >> 2, tig = lane & 3;
-  // warp -> row tile rt (nodes j in {2rt, 2rt+1}, i = 0..7 of every plane) and
-  // output-channel half nb (channels 8 nb .. 8 nb + 7)
-  const int rt = warp & 3, nb = warp >> 2;
   const uint16_t* W = reinterpret_cast<const uint16_t*>(Wbf);
   if (tid < 8) reinterpret_cast<uint32_t*>(smem + kSmZero)[tid] = 0u;
 
-  // weight fragments of this warp's channel half, loaded once.  B[k][n] of
-  // mma.m16n8k16: registers {k = 2 tig, 2 tig + 1} and {k = 2 tig + 8, 2 tig + 9},
-  // column n = g.
-  uint32_t B1[2][2], B2[kTaps][2], B3[2][2];
-  const int co = nb * 8 + g;
+  // weight fragments, loaded once.  B[k][n] of mma.m16n8k16: registers
+  // {k = 2 tig, 2 tig + 1} and {k = 2 tig + 8, 2 tig + 9}, column n = g.
+  uint32_t B1[2][2][2], B2[kTaps][2][2], B3[4][2];
 #pragma unroll
   for (int ks = 0; ks < 2; ++ks)
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int t = ks * 16 + 2 * tig + 8 * h;
-      B1[ks][h] = wpair(W, co * kTaps + t, co * kTaps + t + 1, t < kTaps, t + 1 < kTaps);
-    }
+    for (int nb = 0; nb < 2; ++nb)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int t = ks * 16 + 2 * tig + 8 * h, co = nb * 8 + g;
+        B1[ks][nb][h] = wpair(W, co * kTaps + t, co * kTaps + t + 1, t < kTaps, t + 1 < kTaps);
+      }
 #pragma unroll
   for (int t = 0; t < kTaps; ++t)
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int ci = 2 * tig + 8 * h;
-      B2[t][h] = wpair(W, kO2 + (co * 16 + ci) * kTaps + t, kO2 + (co * 16 + ci + 1) * kTaps + t,
-                       true, true);
-    }
-  // layer 3 has N = 32 tap columns: this warp takes column blocks 2 nb, 2 nb + 1
+    for (int nb = 0; nb < 2; ++nb)
 #pragma unroll
-  for (int b = 0; b < 2; ++b)
+      for (int h = 0; h < 2; ++h) {
+        const int ci = 2 * tig + 8 * h, co = nb * 8 + g;
+        B2[t][nb][h] = wpair(W, kO2 + (co * 16 + ci) * kTaps + t, kO2 + (co * 16 + ci + 1) * kTaps + t,
+                             true, true);
+      }
+#pragma unroll
+  for (int nb = 0; nb < 4; ++nb)
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
-      const int ci = 2 * tig + 8 * h, t = (2 * nb + b) * 8 + g;
-      B3[b][h] = wpair(W, kO3 + ci * kTaps + t, kO3 + (ci + 1) * kTaps + t, t < kTaps, t < kTaps);
+      const int ci = 2 * tig + 8 * h, t = nb * 8 + g;
+      B3[nb][h] = wpair(W, kO3 + ci * kTaps + t, kO3 + (ci + 1) * kTaps + t, t < kTaps, t < kTaps);
     }
 
-  // this lane's ldmatrix row: matrix m = lane/8 -> rows j = 2 rt + (m&1), i = lane%8,
+  // this lane's ldmatrix row: matrix m = lane/8 -> rows j = 2w + (m&1), i = lane%8,
   // channel half m>>1
-  const int lm = lane >> 3, li = lane & 7, lj = 2 * rt + (lm & 1), lhalf = lm >> 1;
-  // this thread's accumulator rows: i = g, j = 2 rt (c0,c1) and 2 rt + 1 (c2,c3)
-  const int jA = 2 * rt, jB = 2 * rt + 1;
+  const int lm = lane >> 3, li = lane & 7, lj = 2 * warp + (lm & 1), lhalf = lm >> 1;
+  // this thread's accumulator rows: i = g, j = 2w (c0,c1) and 2w+1 (c2,c3)
+  const int jA = 2 * warp, jB = 2 * warp + 1;
 
   for (int64_t e = blockIdx.x; e < Etot; e += gridDim.x) {
     // ---- scaled input: a0 = h r / s
@@ -169,7 +162,7 @@ k_net_infer_tc(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ W
       ss += v * v;
     }
     float s = 1.f;
-    if (normalize & kNetNormalize) s = sqrtf(block_sum8(ss, red) / kNp);
+    if (normalize & kNetNormalize) s = sqrtf(block_sum4(ss, red) / kNp);
     const float inv = s > 0.f ? 1.f / s : 0.f;
 #pragma unroll
     for (int c = 0; c < kNp / kThreads; ++c) {
@@ -203,7 +196,7 @@ k_net_infer_tc(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ W
         va[h] = (kok && ((okA >> h) & 1u)) ? a0[nA0 + toff[h]] : 0.f;
         vb[h] = (kok && ((okB >> h) & 1u)) ? a0[nB0 + toff[h]] : 0.f;
       }
-      float acc[4] = {};
+      float acc[2][4] = {};
 #pragma unroll
       for (int ks = 0; ks < 2; ++ks) {
         uint32_t A[4];
@@ -211,21 +204,28 @@ k_net_infer_tc(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ W
         A[1] = pack2(vb[4 * ks + 0], vb[4 * ks + 1]);
         A[2] = pack2(va[4 * ks + 2], va[4 * ks + 3]);
         A[3] = pack2(vb[4 * ks + 2], vb[4 * ks + 3]);
-        mma16816(acc, A, B1[ks][0], B1[ks][1]);
+#pragma unroll
+        for (int nb = 0; nb < 2; ++nb) mma16816(acc[nb], A, B1[ks][nb][0], B1[ks][nb][1]);
       }
-      *reinterpret_cast<uint32_t*>(smem + kSmAct + act_off(nA0, nb) + 4 * tig) =
-          pack2(gelu_tc(acc[0]), gelu_tc(acc[1]));
-      *reinterpret_cast<uint32_t*>(smem + kSmAct + act_off(nB0, nb) + 4 * tig) =
-          pack2(gelu_tc(acc[2]), gelu_tc(acc[3]));
+      const int nA = g + kNq * jA + kNq * kNq * k, nB = g + kNq * jB + kNq * kNq * k;
+#pragma unroll
+      for (int nb = 0; nb < 2; ++nb) {
+        *reinterpret_cast<uint32_t*>(smem + kSmAct + act_off(nA, nb) + 4 * tig) =
+            pack2(gelu_tc(acc[nb][0]), gelu_tc(acc[nb][1]));
+        *reinterpret_cast<uint32_t*>(smem + kSmAct + act_off(nB, nb) + 4 * tig) =
+            pack2(gelu_tc(acc[nb][2]), gelu_tc(acc[nb][3]));
+      }
     }
     __syncthreads();
 
-    // ---- layer 2: this warp's channel half of all 8 planes in registers
-    float acc[kNq][4];
+    // ---- layer 2: accumulators of all 8 planes in registers
+    float acc[kNq][2][4];
 #pragma unroll
     for (int q = 0; q < kNq; ++q)
 #pragma unroll
-      for (int c = 0; c < 4; ++c) acc[q][c] = 0.f;
+      for (int nb = 0; nb < 2; ++nb)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[q][nb][c] = 0.f;
 #pragma unroll
     for (int p = 0; p < kNq; ++p) {
 #pragma unroll
@@ -242,7 +242,8 @@ k_net_infer_tc(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ W
             const int q = p - dk;
             if (q < 0 || q >= kNq) continue;
             const int t = (di + 1) + 3 * (dj + 1) + 9 * (dk + 1);
-            mma16816(acc[q], A, B2[t][0], B2[t][1]);
+            mma16816(acc[q][0], A, B2[t][0][0], B2[t][0][1]);
+            mma16816(acc[q][1], A, B2[t][1][0], B2[t][1][1]);
           }
         }
       }
@@ -251,32 +252,35 @@ k_net_infer_tc(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ W
 #pragma unroll
     for (int q = 0; q < kNq; ++q) {
       const int nA = g + kNq * jA + kNq * kNq * q, nB = g + kNq * jB + kNq * kNq * q;
-      *reinterpret_cast<uint32_t*>(smem + kSmAct + act_off(nA, nb) + 4 * tig) =
-          pack2(gelu_tc(acc[q][0]), gelu_tc(acc[q][1]));
-      *reinterpret_cast<uint32_t*>(smem + kSmAct + act_off(nB, nb) + 4 * tig) =
-          pack2(gelu_tc(acc[q][2]), gelu_tc(acc[q][3]));
+#pragma unroll
+      for (int nb = 0; nb < 2; ++nb) {
+        *reinterpret_cast<uint32_t*>(smem + kSmAct + act_off(nA, nb) + 4 * tig) =
+            pack2(gelu_tc(acc[q][nb][0]), gelu_tc(acc[q][nb][1]));
+        *reinterpret_cast<uint32_t*>(smem + kSmAct + act_off(nB, nb) + 4 * tig) =
+            pack2(gelu_tc(acc[q][nb][2]), gelu_tc(acc[q][nb][3]));
+      }
     }
     __syncthreads();
 
-    // ---- layer 3: U[t][n] = sum_ci act[n][ci] W3[ci][t], this warp's 16 tap columns
+    // ---- layer 3: U[t][n] = sum_ci act[n][ci] W3[ci][t]
 #pragma unroll 1
     for (int k = 0; k < kNq; ++k) {
       uint32_t A[4];
       ldsm_x4(act_s + act_off(li + kNq * lj + kNq * kNq * k, lhalf), A);
-      float u[2][4] = {};
+      float u[4][4] = {};
 #pragma unroll
-      for (int b = 0; b < 2; ++b) mma16816(u[b], A, B3[b][0], B3[b][1]);
+      for (int nb = 0; nb < 4; ++nb) mma16816(u[nb], A, B3[nb][0], B3[nb][1]);
       const int nA = g + kNq * jA + kNq * kNq * k, nB = g + kNq * jB + kNq * kNq * k;
 #pragma unroll
-      for (int b = 0; b < 2; ++b) {
-        const int t = (2 * nb + b) * 8 + 2 * tig;
+      for (int nb = 0; nb < 4; ++nb) {
+        const int t = nb * 8 + 2 * tig;
         if (t < kTaps) {
-          U[t * kUStride + nA] = u[b][0];
-          U[t * kUStride + nB] = u[b][2];
+          U[t * kUStride + nA] = u[nb][0];
+          U[t * kUStride + nB] = u[nb][2];
         }
         if (t + 1 < kTaps) {
-          U[(t + 1) * kUStride + nA] = u[b][1];
-          U[(t + 1) * kUStride + nB] = u[b][3];
+          U[(t + 1) * kUStride + nA] = u[nb][1];
+          U[(t + 1) * kUStride + nB] = u[nb][3];
         }
       }
     }
