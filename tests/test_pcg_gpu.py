@@ -250,3 +250,21 @@ def test_zero_mean_entry(nb, O, dev):
     torch.cuda.synchronize()
     want = O.zero_mean(q0.copy(), bp.Nlocal, Nfields=3, offset=bp.offset)
     assert np.abs(q.cpu().numpy() - want).max() <= 1e-14
+
+
+def test_nekbone_driver_bp_mode_and_helmholtz(nb, dev):
+    """The nekBone driver: BP mode on the reference's BP5 case reproduces its
+    correctness check (78 iterations, maxError 1.03e-7, within one iteration and
+    10 %); the Dirichlet Helmholtz problem converges with the FP64 and mixed
+    solvers and reports the reference's throughput figures."""
+    from nekbench_gb300 import nekbone
+    out = nekbone.main(["--bp-mode", "--nx", "16", "--ny", "16", "--nz", "32", "--tol", "1e-6",
+                        "--maxit", "1000", "--json"])
+    assert abs(out["check"]["iterations"] - 78) <= 1
+    assert abs(out["check"]["max_error"] - 1.02763e-07) <= 0.10 * 1.02763e-07
+    assert out["gdofs_per_iter"] > 0 and out["bandwidth_gbs"] > 0
+    for solver in ("fp64", "mixed"):
+        out = nekbone.main(["--nx", "4", "--ny", "4", "--nz", "4", "--solver", solver, "--json"])
+        assert out["status"] == 0 and out["true_rel_res"] <= 1e-8
+    out = nekbone.main(["--nx", "4", "--ny", "4", "--nz", "4", "--fixed", "--maxit", "50", "--json"])
+    assert out["iterations"] == 50
