@@ -1180,7 +1180,7 @@ int solve_mixed(nekb_bp* bp, const double* lambda, double* r, double* x, double 
     total = it + done_before;
     if (st == NEKB_ERR_BREAKDOWN) status = st;
   }
-  if (rdotr > TOL && status == NEKB_OK) status = NEKB_ERR_NOT_CONVERGED;
+  if (rdotr > TOL && status == NEKB_OK && !o.fixed_iterations) status = NEKB_ERR_NOT_CONVERGED;
   stats->iterations = total;
   stats->outer_iterations = outer;
   stats->status = status;

@@ -266,5 +266,7 @@ def test_nekbone_driver_bp_mode_and_helmholtz(nb, dev):
     for solver in ("fp64", "mixed"):
         out = nekbone.main(["--nx", "4", "--ny", "4", "--nz", "4", "--solver", solver, "--json"])
         assert out["status"] == 0 and out["true_rel_res"] <= 1e-8
-    out = nekbone.main(["--nx", "4", "--ny", "4", "--nz", "4", "--fixed", "--maxit", "50", "--json"])
-    assert out["iterations"] == 50
+    for solver in ("fp64", "mixed"):
+        out = nekbone.main(["--nx", "4", "--ny", "4", "--nz", "4", "--solver", solver, "--fixed",
+                            "--maxit", "50", "--json"])
+        assert out["iterations"] == 50 and out["status"] == 0
