@@ -215,6 +215,13 @@ __global__ void k_trilinear_coeffs(int64_t E, const double* __restrict__ EX,
 // the groups that have more than one member (singleton groups are a no-op in
 // the reference).  One thread per (group, field); the sum runs over the
 // members in CSR order, so results are deterministic and equal to the CPU's.
+//
+// The kernel is bound by the latency of three dependent loads per group
+// (offsets -> ids -> values), so each thread takes kGsGroups groups at a time
+// and issues the loads of all of them (offsets, then the first two member ids,
+// then their values) before it sums; the members are still added in CSR order.
+constexpr int kGsGroups = 4;
+
 template <typename T>
 __global__ void k_gs_add(int64_t Ngroups, const int32_t* __restrict__ offsets,
                          const int32_t* __restrict__ ids, int k, int64_t stride, T* __restrict__ q,
@@ -222,15 +229,44 @@ __global__ void k_gs_add(int64_t Ngroups, const int32_t* __restrict__ offsets,
 {
   if (skip != nullptr && *skip != 0) return;
   const int64_t total = Ngroups * k;
-  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total;
-       g += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t f = g / Ngroups;
-    const int64_t gid = g - f * Ngroups;
-    T* qf = q + f * stride;
-    const int32_t start = offsets[gid], end = offsets[gid + 1];
-    T s = 0;
-    for (int32_t n = start; n < end; ++n) s += qf[ids[n]];
-    for (int32_t n = start; n < end; ++n) qf[ids[n]] = s;
+  const int64_t step = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t g0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g0 < total;
+       g0 += kGsGroups * step) {
+    int32_t st[kGsGroups], en[kGsGroups], i0[kGsGroups], i1[kGsGroups];
+    T* qf[kGsGroups];
+#pragma unroll
+    for (int u = 0; u < kGsGroups; ++u) {
+      const int64_t g = g0 + u * step;
+      st[u] = en[u] = 0;
+      qf[u] = q;
+      if (g < total) {
+        const int64_t f = g / Ngroups, gid = g - f * Ngroups;
+        qf[u] = q + f * stride;
+        st[u] = offsets[gid];
+        en[u] = offsets[gid + 1];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kGsGroups; ++u) {
+      i0[u] = st[u] < en[u] ? ids[st[u]] : -1;
+      i1[u] = st[u] + 1 < en[u] ? ids[st[u] + 1] : -1;
+    }
+    T s[kGsGroups];
+#pragma unroll
+    for (int u = 0; u < kGsGroups; ++u) {
+      const T a = i0[u] >= 0 ? qf[u][i0[u]] : T(0);
+      const T b = i1[u] >= 0 ? qf[u][i1[u]] : T(0);
+      s[u] = a + b;  // (0 + a) + b: the CSR-order sum of the first two members
+    }
+#pragma unroll
+    for (int u = 0; u < kGsGroups; ++u)
+      for (int32_t n = st[u] + 2; n < en[u]; ++n) s[u] += qf[u][ids[n]];
+#pragma unroll
+    for (int u = 0; u < kGsGroups; ++u) {
+      if (i0[u] >= 0) qf[u][i0[u]] = s[u];
+      if (i1[u] >= 0) qf[u][i1[u]] = s[u];
+      for (int32_t n = st[u] + 2; n < en[u]; ++n) qf[u][ids[n]] = s[u];
+    }
   }
 }
 
@@ -360,10 +396,10 @@ int launch_gs_add(int64_t Ngroups, const int32_t* offsets, const int32_t* ids, i
   const int64_t n = Ngroups * k;
   if (n == 0) return NEKB_OK;
   if (dtype == NEKB_DOUBLE)
-    k_gs_add<double><<<grid_for(n, 256, 152 * 32), 256, 0, s>>>(Ngroups, offsets, ids, k, stride,
+    k_gs_add<double><<<grid_for((n + kGsGroups - 1) / kGsGroups, 256, 152 * 32), 256, 0, s>>>(Ngroups, offsets, ids, k, stride,
                                                                   (double*)q, skip);
   else if (dtype == NEKB_FLOAT)
-    k_gs_add<float><<<grid_for(n, 256, 152 * 32), 256, 0, s>>>(Ngroups, offsets, ids, k, stride,
+    k_gs_add<float><<<grid_for((n + kGsGroups - 1) / kGsGroups, 256, 152 * 32), 256, 0, s>>>(Ngroups, offsets, ids, k, stride,
                                                                  (float*)q, skip);
   else
     return fail(NEKB_ERR_UNSUPPORTED, "gather-scatter: dtype %d", dtype);
