@@ -318,7 +318,7 @@ def pcg_comparison(nb, torch, dev, n, learned):
     if learned:
         net = learned_net(nb, torch, dev)
         if net is not None:
-            runs.append(("mixed_learned", dict(solver=nb.SOLVER_MIXED, inner_precision=nb.FP32_TRILINEAR,
+            runs.append(("mixed_learned", dict(solver=nb.SOLVER_MIXED, inner_precision=nb.FP32,
                                                precond=nb.PRECOND_LEARNED, net=net)))
     r, x = torch.empty_like(f), torch.empty_like(f)
     for name, kw in runs:

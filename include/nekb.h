@@ -208,7 +208,9 @@ typedef struct {
   int flexible;         /* 1: flexible beta (KRYLOV SOLVER FLEXIBLE)            */
   int fixed_iterations; /* 1: run exactly maxit iterations                      */
   int bk;               /* 1: Poisson operator (lambda0=1, lambda1=0)           */
-  int inner_precision;  /* NEKB_FP32, NEKB_BF16 or NEKB_FP32_TRILINEAR (mixed)  */
+  int inner_precision;  /* NEKB_FP32 (default), NEKB_BF16 or NEKB_FP32_TRILINEAR
+                           (mixed; the trilinear form keeps no FP32 geometry,
+                           28 B/node less, at about 7 % more time)           */
   double inner_tol;     /* mixed: residual reduction between two replacements of
                            the FP32 residual by the true FP64 one (1e-2)       */
   int max_outer;        /* mixed: limit on FP64 residual replacements           */

@@ -435,7 +435,7 @@ class BP:
                                              _ptr(inv_diag), _ptr(y), int(iters), float(tol)))
 
     def pcg(self, lam, r, x, tol, maxit, solver=SOLVER_FP64, precond=PRECOND_JACOBI,
-            flexible=False, fixed_iterations=False, bk=False, inner_precision=FP32_TRILINEAR,
+            flexible=False, fixed_iterations=False, bk=False, inner_precision=FP32,
             inner_tol=1e-2, max_outer=40, check_every=16, use_graph=True, net=None,
             zero_mean=False, fcg_window=0):
         """BPPCG: r (rhs in, residual out) and x (guess in, solution out) are device FP64;

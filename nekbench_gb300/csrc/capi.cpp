@@ -345,7 +345,7 @@ void nekb_pcg_default_opts(nekb_pcg_opts* o)
   std::memset(o, 0, sizeof(*o));
   o->solver = NEKB_SOLVER_FP64;
   o->precond = NEKB_PRECOND_JACOBI;
-  o->inner_precision = NEKB_FP32_TRILINEAR;
+  o->inner_precision = NEKB_FP32;
   o->inner_tol = 1e-2;
   o->max_outer = 20;
   o->check_every = 16;

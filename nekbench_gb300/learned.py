@@ -160,7 +160,7 @@ def evaluate(bp, net, seeds, torch, dev, tol=1e-8, inner_precision=None, solver=
              fcg_window=0):
     """Iterations and time to `tol` (true FP64 relative residual) with and without
     the network, on the same problems."""
-    inner_precision = nb.FP32_TRILINEAR if inner_precision is None else inner_precision
+    inner_precision = nb.FP32 if inner_precision is None else inner_precision
     solver = nb.SOLVER_MIXED if solver is None else solver
     r = torch.empty(bp.Nlocal, dtype=torch.float64, device=dev)
     x = torch.empty_like(r)
