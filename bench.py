@@ -311,6 +311,7 @@ def pcg_comparison(nb, torch, dev, n, learned):
                        f"lambda1~U[0.5,2.0], f~U[-1,1] assembled; stop at true FP64 "
                        f"relative residual 1e-8", "E": bp.E, "unknowns_local": L}
     runs = [("fp64_jacobi", dict(solver=nb.SOLVER_FP64)),
+            ("fp64_split_jacobi", dict(solver=nb.SOLVER_FP64_SPLIT)),
             ("mixed_fp32_trilinear", dict(solver=nb.SOLVER_MIXED, inner_precision=nb.FP32_TRILINEAR)),
             ("mixed_fp32", dict(solver=nb.SOLVER_MIXED, inner_precision=nb.FP32)),
             ("mixed_bf16", dict(solver=nb.SOLVER_MIXED, inner_precision=nb.BF16))]

@@ -201,6 +201,8 @@ int nekb_bp_zero_mean(nekb_bp* bp, double* q);
 
 #define NEKB_SOLVER_FP64     0   /* plain FP64 PCG (the reference algorithm)          */
 #define NEKB_SOLVER_MIXED    1   /* FP32/BF16 inner PCG inside FP64 iterative refinement */
+#define NEKB_SOLVER_FP64_SPLIT 2 /* the FP64 PCG with the double-float operator
+                                    (NEKB_FP64_SPLIT; FP64 vectors and sums)       */
 
 typedef struct {
   int solver;           /* NEKB_SOLVER_*                                        */

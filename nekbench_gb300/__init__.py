@@ -28,7 +28,7 @@ AX_BK, AX_N3, AX_PARTIAL = 1, 2, 4
 FP64, FP32, BF16, FP32_TRILINEAR, FP64_SPLIT = 0, 1, 2, 3, 4
 DOUBLE, FLOAT = 0, 1
 PRECOND_COPY, PRECOND_JACOBI, PRECOND_LEARNED = 0, 1, 2
-SOLVER_FP64, SOLVER_MIXED = 0, 1
+SOLVER_FP64, SOLVER_MIXED, SOLVER_FP64_SPLIT = 0, 1, 2
 NET_FP32, NET_TENSOR = 0, 1
 OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_UNSUPPORTED, ERR_BREAKDOWN, ERR_NOT_CONVERGED = \
     0, -1, -2, -3, -4, -5, -6

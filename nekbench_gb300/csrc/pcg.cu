@@ -995,7 +995,10 @@ int solve_fp64(nekb_bp* bp, const double* lambda, double* r, double* x, double t
   const int64_t Nall = bp->Nfields * bp->offset;
   if (!o.bk && lambda == nullptr) return fail(NEKB_ERR_INVALID, "PCG: lambda is NULL for a Helmholtz solve");
   if (o.precond == NEKB_PRECOND_LEARNED) return fail(NEKB_ERR_UNSUPPORTED, "learned preconditioner needs the mixed solver");
-  OpView op = make_op(bp, o.bk, NEKB_FP64, lambda);
+  // the Krylov operator: native FP64, or double-float on the FP32 pipes
+  // (NEKB_SOLVER_FP64_SPLIT); the final true residual always uses native FP64
+  const OpView op64 = make_op(bp, o.bk, NEKB_FP64, lambda);
+  const OpView op = o.solver == NEKB_SOLVER_FP64_SPLIT ? make_op(bp, o.bk, NEKB_FP64_SPLIT, lambda) : op64;
   NEKB_TRY(bp->b.ensure(sizeof(double) * Nall));
   NEKB_TRY(bp->rr.ensure(sizeof(double) * Nall));
   NEKB_TRY(mask_rhs_guess(bp, r, x));
@@ -1010,7 +1013,7 @@ int solve_fp64(nekb_bp* bp, const double* lambda, double* r, double* x, double t
                             o.fixed_iterations != 0, o.check_every, o.use_graph != 0, nullptr,
                             &iters, &status, &rdotr0, &rdotr));
   // true FP64 residual |b - A x|_w / |b - A x0|_w
-  NEKB_TRY(apply_op(op, x, bp->Ax.p, nullptr, s));
+  NEKB_TRY(apply_op(op64, x, bp->Ax.p, nullptr, s));
   k_residual<<<vec_grid(Nall), RT, 0, s>>>(Nall, bp->b.as<double>(), bp->Ax.as<double>(), bp->rr.as<double>());
   NEKB_CUDA(cudaGetLastError());
   double tr = 0;
@@ -1205,6 +1208,8 @@ int bp_pcg(nekb_bp* bp, const double* lambda, double* r, double* x, double tol, 
   if (!bp || !r || !x || !stats) return fail(NEKB_ERR_INVALID, "PCG: NULL argument");
   if (maxit < 0 || !(tol >= 0)) return fail(NEKB_ERR_INVALID, "PCG: maxit=%d tol=%g", maxit, tol);
   if (o.check_every <= 0) o.check_every = 16;
+  if (o.solver != NEKB_SOLVER_FP64 && o.solver != NEKB_SOLVER_MIXED && o.solver != NEKB_SOLVER_FP64_SPLIT)
+    return fail(NEKB_ERR_INVALID, "PCG: unknown solver %d", o.solver);
   cudaEvent_t e0, e1;
   NEKB_CUDA(cudaEventCreate(&e0));
   NEKB_CUDA(cudaEventCreate(&e1));

@@ -2,7 +2,7 @@
 check and timed solves, with the reference's summary (nekBone/main.cpp:35-230).
 
   python -m nekbench_gb300.nekbone [--bp-mode] [--nx 16 --ny 16 --nz 32] [--N 7]
-      [--nfields 1] [--solver fp64|mixed] [--inner fp32|bf16|fp32_trilinear]
+      [--nfields 1] [--solver fp64|fp64_split|mixed] [--inner fp32|bf16|fp32_trilinear]
       [--precond jacobi|copy|learned] [--tol 1e-8] [--maxit 1000] [--fixed]
       [--repetitions 1]
 
@@ -35,7 +35,7 @@ def parse(argv=None):
     p.add_argument("--nz", type=int, default=32)
     p.add_argument("--N", type=int, default=7)
     p.add_argument("--nfields", type=int, default=1, choices=(1, 3))
-    p.add_argument("--solver", default="fp64", choices=("fp64", "mixed"))
+    p.add_argument("--solver", default="fp64", choices=("fp64", "fp64_split", "mixed"))
     p.add_argument("--inner", default="fp32", choices=("fp32", "bf16", "fp32_trilinear"))
     p.add_argument("--precond", default=None, choices=("jacobi", "copy", "learned"))
     p.add_argument("--weights", default=os.path.join(os.path.dirname(os.path.abspath(__file__)),
@@ -90,7 +90,8 @@ def main(argv=None):
         f = torch.empty(a.nfields * L, dtype=torch.float64, device=dev)
         nb.fill_uniform(f, a.seed, 3, -1.0, 1.0)
     bp.ogs.gather_scatter_many(f, k=a.nfields, stride=L)
-    kw = dict(solver=nb.SOLVER_MIXED if a.solver == "mixed" else nb.SOLVER_FP64,
+    kw = dict(solver={"fp64": nb.SOLVER_FP64, "fp64_split": nb.SOLVER_FP64_SPLIT,
+                      "mixed": nb.SOLVER_MIXED}[a.solver],
               precond={"jacobi": nb.PRECOND_JACOBI, "copy": nb.PRECOND_COPY,
                        "learned": nb.PRECOND_LEARNED}[precond],
               bk=a.bp_mode, zero_mean=a.bp_mode,

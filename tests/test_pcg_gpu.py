@@ -270,3 +270,21 @@ def test_nekbone_driver_bp_mode_and_helmholtz(nb, dev):
         out = nekbone.main(["--nx", "4", "--ny", "4", "--nz", "4", "--solver", solver, "--fixed",
                             "--maxit", "50", "--json"])
         assert out["iterations"] == 50 and out["status"] == 0
+
+
+def test_fp64_pcg_with_the_double_float_operator(nb, O, dev):
+    """The FP64 PCG with the double-float operator (FP64 vectors and sums): the
+    oracle's iteration count within one and its solution within 1e-7, true
+    FP64 residual at the tolerance; an unknown solver is refused."""
+    bp, m = pair(nb, O, 7, 4)
+    obp, lam, f = problem(O, m, 1, 11)
+    r_h, x_h = f.copy(), np.zeros_like(f)
+    it_o = obp.pcg(r_h, x_h, 1e-8, 500, precond=1)
+    r_d, x_d = T(f, dev), torch.zeros(len(f), dtype=torch.float64, device=dev)
+    st = bp.pcg(T(lam, dev), r_d, x_d, 1e-8, 500, solver=nb.SOLVER_FP64_SPLIT)
+    assert st["status"] == 0 and abs(st["iterations"] - it_o) <= 1, (st, it_o)
+    assert rel(x_d.cpu().numpy(), x_h) < 1e-7
+    assert true_rel_res(obp, f, x_d.cpu().numpy()) < 1.05e-8
+    with pytest.raises(nb.NekbError):
+        bp.pcg(T(lam, dev), T(f, dev), torch.zeros(len(f), dtype=torch.float64, device=dev),
+               1e-8, 10, solver=7)
