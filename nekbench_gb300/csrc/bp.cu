@@ -55,7 +55,8 @@ int apply_op(const OpView& op, const void* q, void* Aq, const int* skip, cudaStr
     a.w1d[i] = op.w1d[i];
   }
   NEKB_TRY(launch_axhelm(op.Nq, op.flags, op.precision, a, s));
-  const int dtype = op.precision == NEKB_FP64 ? NEKB_DOUBLE : NEKB_FLOAT;
+  const bool fp64 = op.precision == NEKB_FP64 || op.precision == NEKB_FP64_SPLIT;
+  const int dtype = fp64 ? NEKB_DOUBLE : NEKB_FLOAT;
   NEKB_TRY(launch_gs_add(op.ogs->Nmulti, op.ogs->d_offsets, op.ogs->d_ids, op.Nfields, op.offset,
                          Aq, dtype, skip, s));
   NEKB_TRY(launch_mask(op.Nmasked, op.mask, op.Nfields, op.offset, Aq, dtype, skip, s));
