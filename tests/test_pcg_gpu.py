@@ -288,3 +288,18 @@ def test_fp64_pcg_with_the_double_float_operator(nb, O, dev):
     with pytest.raises(nb.NekbError):
         bp.pcg(T(lam, dev), T(f, dev), torch.zeros(len(f), dtype=torch.float64, device=dev),
                1e-8, 10, solver=7)
+
+
+@pytest.mark.parametrize("bk", [False, True])
+def test_assembled_operator_in_double_float(nb, O, dev, bk):
+    """mask(gs(axhelm(q))) with the double-float operator equals the native FP64
+    one to 1e-12 (the assembly runs on FP64 values in both)."""
+    bp, m = pair(nb, O, 7, 3)
+    L = bp.Nlocal
+    lam = T(np.concatenate([O.uniform(L, 31, 1, 0.5, 1.5), O.uniform(L, 31, 2, 0.5, 2.0)]), dev)
+    q = T(O.uniform(L, 31, 3, -1, 1), dev)
+    bp.ogs.gather_scatter_many(q)
+    a64, a2 = torch.empty_like(q), torch.empty_like(q)
+    bp.apply(q, a64, lam, bk=bk, precision=nb.FP64)
+    bp.apply(q, a2, lam, bk=bk, precision=nb.FP64_SPLIT)
+    assert rel(a2.cpu().numpy(), a64.cpu().numpy()) < 1e-12
