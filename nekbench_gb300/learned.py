@@ -33,7 +33,6 @@ import numpy as np
 
 import nekbench_gb300 as nb
 
-SNAPSHOTS = (0, 10, 40, 120)
 # residual snapshots spread over a whole Jacobi-PCG solve (fractions of its
 # iteration count): late residuals are smooth across elements and must be in
 # the training set too
