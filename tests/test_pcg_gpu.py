@@ -313,8 +313,7 @@ def test_vector_helmholtz_mixed_to_1e10_at_full_size(nb, dev, N):
     assembled.  FP32 and BF16-storage inner operators inside the FP64 residual
     replacement reach a true FP64 relative residual of 1e-10; their solutions
     agree with the plain FP64 PCG's (itself checked against the oracle at small
-    sizes) to 1e-6 relative (residuals of 1e-10 bound the error by the
-    condition number times 1e-10)."""
+    sizes) to 1e-7 relative (measured: FP32 2e-10 / 1e-9, BF16 9e-9 at N=7 / 9)."""
     bp = nb.BP(N, 32, 32, 32, Nfields=3, perturb=0.1, seed=17)
     L = bp.Nlocal
     lam = torch.empty(2 * L, dtype=torch.float64, device=dev)
@@ -335,5 +334,5 @@ def test_vector_helmholtz_mixed_to_1e10_at_full_size(nb, dev, N):
     for name in ("fp32", "bf16"):
         err = float((sols[name] - ref).norm() / ref.norm())
         print(f"N={N} {name}: relative difference to the FP64 solution {err:.2e}")
-        assert err <= 1e-6, (name, err)
+        assert err <= 1e-7, (name, err)
     bp.free()
