@@ -336,3 +336,23 @@ def test_vector_helmholtz_mixed_to_1e10_at_full_size(nb, dev, N):
         print(f"N={N} {name}: relative difference to the FP64 solution {err:.2e}")
         assert err <= 1e-7, (name, err)
     bp.free()
+
+
+@pytest.mark.timeout(600)
+def test_nekbone_configuration_against_the_oracle(nb, O, dev):
+    """The nekBone PCG configuration at its stated size: N=7, E=16^3=4096,
+    homogeneous Dirichlet, f ~ U[-1,1] assembled, Jacobi from the assembled
+    diagonal, 100 iterations; the GPU solution and residual agree with the
+    oracle's after the same 100 iterations (1e-8 relative: 100 steps of two
+    summation orders)."""
+    bp, m = pair(nb, O, 7, 16)
+    L = m.Nlocal
+    obp, lam, f = problem(O, m, 1, 21, bk=False)
+    obp = O.BP(m, np.concatenate([np.ones(L), np.zeros(L)]), bk=True)
+    r_h, x_h = f.copy(), np.zeros_like(f)
+    it_o = obp.pcg(r_h, x_h, 0.0, 100, precond=1, fixed=True)
+    r_d, x_d = T(f, dev), torch.zeros(L, dtype=torch.float64, device=dev)
+    st = bp.pcg(None, r_d, x_d, 0.0, 100, fixed_iterations=True, bk=True)
+    assert it_o == 100 and st["iterations"] == 100 and st["status"] == 0
+    assert rel(x_d.cpu().numpy(), x_h) < 1e-8
+    assert rel(r_d.cpu().numpy(), r_h) < 1e-6
