@@ -296,7 +296,9 @@ int nekb_net_num_params(const nekb_net* net);
 /* FP32 master weights (host arrays of nekb_net_num_params floats) */
 int nekb_net_get_weights(const nekb_net* net, float* w);
 int nekb_net_set_weights(nekb_net* net, const float* w);
-/* forward on E element blocks: in/out device float [E][Nq^3] */
+/* forward on E element blocks: in/out device float [E][Nq^3]; with the
+ * tensor-core inference the arrays must be 16-byte aligned (whole element rows
+ * are fetched by bulk copies) and the call returns once the stream is done */
 int nekb_net_forward(nekb_net* net, int64_t E, const float* in, float* out, void* stream);
 /* one training step on a batch: loss = mean_e |net(in_e) - target_e|^2 / Np;
  * computes gradients with the network's own backward kernels and applies Adam.

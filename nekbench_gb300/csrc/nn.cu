@@ -750,7 +750,13 @@ int nekb_net_forward(nekb_net* net, int64_t E, const float* in, float* out, void
 {
   if (!net || (E > 0 && (!in || !out)) || E < 0) return fail(NEKB_ERR_INVALID, "net forward: bad arguments");
   if (E == 0) return NEKB_OK;
-  return net_infer(net, E, E, in, nullptr, nullptr, out, 0, nullptr, static_cast<cudaStream_t>(stream));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  NEKB_TRY(net_infer(net, E, E, in, nullptr, nullptr, out, 0, nullptr, s));
+  if (nekb_net_inference(net) == NEKB_NET_TENSOR) {
+    NEKB_CUDA(cudaStreamSynchronize(s));
+    return net_tc_copy_timeout();
+  }
+  return NEKB_OK;
 }
 
 int nekb_net_gradient(nekb_net* net, int64_t E, const float* in, const float* target, float* grad,

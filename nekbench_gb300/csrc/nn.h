@@ -22,5 +22,8 @@ bool net_tc_supported(int Nq, int C);
 int net_infer_tc(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const float* r,
                  const float* w, const float* invDiag, float* out, int normalize, const int* skip,
                  cudaStream_t s);
+// NEKB_OK, or an error (and the flag cleared) when a tensor-core launch gave up
+// waiting for its input copies since the last call
+int net_tc_copy_timeout();
 
 }  // namespace nekb

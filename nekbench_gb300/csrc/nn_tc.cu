@@ -37,7 +37,14 @@ constexpr int kSmA0 = kSmZero + 32;                      // scaled input, 512 fl
 constexpr int kSmH = kSmA0 + kNp * 4;                    // sqrt(invDiag), 512 floats
 constexpr int kSmU = kSmH + kNp * 4;                     // [27][kUStride] floats
 constexpr int kSmRed = kSmU + kTaps * kUStride * 4;      // block-sum scratch
-constexpr int kSmTotal = kSmRed + 64;
+constexpr int kSmIn = kSmRed + 64;                       // [2 buffers][r, invDiag, w][512] floats
+constexpr int kSmBar = kSmIn + 2 * 3 * kNp * 4;          // two mbarriers
+constexpr int kSmTotal = kSmBar + 16;
+constexpr int kRowBytes = kNp * 4;                       // one element row of a node array
+constexpr long kWaitLimit = 1L << 22;                    // bounded mbarrier waits
+
+// set when an input copy did not complete within kWaitLimit polls
+__device__ int g_tc_copy_timeout;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p)
 {
@@ -83,6 +90,45 @@ __device__ __forceinline__ uint32_t wpair(const uint16_t* W, int i0, int i1, boo
 {
   const uint32_t lo = v0 ? W[i0] : 0u, hi = v1 ? W[i1] : 0u;
   return lo | (hi << 16);
+}
+
+// ---- bulk asynchronous copies of an element's input rows (cp.async.bulk with
+// mbarrier completion): the next element's rows are fetched while the current
+// one is computed
+__device__ __forceinline__ void bar_init(uint32_t bar)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void bar_expect(uint32_t bar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_row(uint32_t dst, const float* src, uint32_t bar)
+{
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::
+          "r"(dst), "l"(src), "r"((uint32_t)kRowBytes), "r"(bar)
+      : "memory");
+}
+
+// true once the barrier has completed the phase with the given parity; false
+// after kWaitLimit polls
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity)
+{
+  for (long it = 0; it < kWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
 }
 
 __device__ __forceinline__ float block_sum4(float v, float* red)
@@ -149,14 +195,54 @@ k_net_infer_tc(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ W
   // this thread's accumulator rows: i = g, j = 2w (c0,c1) and 2w+1 (c2,c3)
   const int jA = 2 * warp, jB = 2 * warp + 1;
 
-  for (int64_t e = blockIdx.x; e < Etot; e += gridDim.x) {
+  // input rows r, invDiag, w of an element: double-buffered in shared memory,
+  // filled by bulk copies that complete on the buffer's mbarrier
+  const float* inb = reinterpret_cast<const float*>(smem + kSmIn);
+  const uint32_t in_s = smem_addr(smem + kSmIn), bar_s = smem_addr(smem + kSmBar);
+  const uint32_t nrows = 1u + (invDiag ? 1u : 0u) + (w ? 1u : 0u);
+  if (tid == 0) {
+    bar_init(bar_s);
+    bar_init(bar_s + 8);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+  }
+  __syncthreads();
+  auto fetch = [&](int64_t el, int buf) {  // one thread issues the copies of element el
+    const uint32_t bar = bar_s + 8 * buf, dst = in_s + buf * 3 * kRowBytes;
+    bar_expect(bar, nrows * kRowBytes);
+    bulk_row(dst, r + el * kNp, bar);
+    if (invDiag) bulk_row(dst + kRowBytes, invDiag + (el % Efield) * kNp, bar);
+    if (w) bulk_row(dst + 2 * kRowBytes, w + (el % Efield) * kNp, bar);
+  };
+  if (tid == 0 && (int64_t)blockIdx.x < Etot) fetch(blockIdx.x, 0);
+  uint32_t parity0 = 0, parity1 = 0;
+  int buf = 0;
+
+  for (int64_t e = blockIdx.x; e < Etot; e += gridDim.x, buf ^= 1) {
+    // the other buffer was released by the previous element's last barrier
+    const bool next = e + gridDim.x < Etot;
+    if (tid == 0 && next) {
+      asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");  // reads of the buffer are done
+      fetch(e + gridDim.x, buf ^ 1);
+    }
+    const bool ok = bar_wait(bar_s + 8 * buf, buf ? parity1 : parity0);
+    if (buf) parity1 ^= 1u; else parity0 ^= 1u;
+    if (__syncthreads_or(!ok)) {  // give up: wait (bounded) for the copy in flight, flag, return
+      if (tid == 0) {
+        if (next) bar_wait(bar_s + 8 * (buf ^ 1), buf ? parity0 : parity1);
+        atomicExch(&g_tc_copy_timeout, 1);
+      }
+      return;
+    }
+    const float* rin = inb + buf * 3 * kNp;
+    const float* din = rin + kNp;
+    const float* win = rin + 2 * kNp;
     // ---- scaled input: a0 = h r / s
     float ss = 0.f;
 #pragma unroll
     for (int c = 0; c < kNp / kThreads; ++c) {
       const int n = tid + c * kThreads;
-      const float h = invDiag ? sqrtf(invDiag[(e % Efield) * kNp + n]) : 1.f;
-      const float v = h * r[e * kNp + n];
+      const float h = invDiag ? sqrtf(din[n]) : 1.f;
+      const float v = h * rin[n];
       hs[n] = h;
       a0[n] = v;
       ss += v * v;
@@ -299,16 +385,28 @@ k_net_infer_tc(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ W
         if (a >= 0 && a < kNq && b >= 0 && b < kNq && cc >= 0 && cc < kNq)
           o += U[t * kUStride + n + di + kNq * dj + kNq * kNq * dk];
       }
-      const float wn = w ? w[(e % Efield) * kNp + n] : 1.f;
+      const float wn = w ? win[n] : 1.f;
       o *= hs[n] * s;
-      if ((normalize & kNetAddJacobi) && invDiag) o += invDiag[(e % Efield) * kNp + n] * r[e * kNp + n];
+      if ((normalize & kNetAddJacobi) && invDiag) o += din[n] * rin[n];
       out[e * kNp + n] = wn * o;
     }
-    __syncthreads();  // U, act and a0 are rewritten for the next element
+    __syncthreads();  // U, act, a0 and this input buffer are rewritten later
   }
 }
 
 }  // namespace
+
+int net_tc_copy_timeout()
+{
+  int flag = 0;
+  NEKB_CUDA(cudaMemcpyFromSymbol(&flag, g_tc_copy_timeout, sizeof(int)));
+  if (flag) {
+    const int zero = 0;
+    NEKB_CUDA(cudaMemcpyToSymbol(g_tc_copy_timeout, &zero, sizeof(int)));
+    return fail(NEKB_ERR_CUDA, "network: an input copy did not complete in time");
+  }
+  return NEKB_OK;
+}
 
 bool net_tc_supported(int Nq, int C) { return Nq == kNq && C == 16; }
 
@@ -316,6 +414,10 @@ int net_infer_tc(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const f
                  const float* w, const float* invDiag, float* out, int normalize, const int* skip,
                  cudaStream_t s)
 {
+  // the bulk copies move whole element rows: 16-byte aligned arrays
+  for (const void* p : {(const void*)r, (const void*)w, (const void*)invDiag})
+    if (reinterpret_cast<uintptr_t>(p) % 16 != 0)
+      return fail(NEKB_ERR_INVALID, "network: input arrays must be 16-byte aligned");
   static bool attr = false;
   if (!attr) {
     NEKB_CUDA(cudaFuncSetAttribute(k_net_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmTotal));

@@ -1181,6 +1181,7 @@ int solve_mixed(nekb_bp* bp, const double* lambda, double* r, double* x, double 
                              o.use_graph != 0,
                              &ext, &it, &st, &a0, &a1, &hook));
     total = it + done_before;
+    if (learned) NEKB_TRY(net_tc_copy_timeout());
     if (st == NEKB_ERR_BREAKDOWN) status = st;
   }
   if (rdotr > TOL && status == NEKB_OK && !o.fixed_iterations) status = NEKB_ERR_NOT_CONVERGED;
