@@ -7,11 +7,22 @@
 
 namespace nekb {
 
+// The Krylov update that precedes the preconditioner in an FCG iteration:
+// x += alpha p, r -= alpha Ap with alpha read from the device.
+struct NetUpdate {
+  const double* alpha;
+  float* x;
+  const float* p;
+  const float* Ap;
+};
+
 // z = Jacobi(r) + mask(gs(w * h * s_e * net(h * r_e / s_e))), h = sqrt(invDiag),
-// s_e = RMS of h * r over element e.
+// s_e = RMS of h * r over element e; with upd, r (and x) are first updated
+// (by the network kernel itself on the tensor-core path).
 // Runs on stream s; returns at once on the device when *skip != 0.
-int net_precondition(nekb_bp* bp, nekb_net* net, const float* r, float* z, const float* invDiag,
-                     const float* w, const int* skip, cudaStream_t s);
+int net_precondition(nekb_bp* bp, nekb_net* net, float* r, float* z, const float* invDiag,
+                     const float* w, const int* skip, cudaStream_t s,
+                     const NetUpdate* upd = nullptr);
 
 // inference mode bits: normalise by the element RMS of sqrt(invDiag) r; add
 // w invDiag r to the output
@@ -21,7 +32,7 @@ constexpr int kNetNormalize = 1, kNetAddJacobi = 2;
 bool net_tc_supported(int Nq, int C);
 int net_infer_tc(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const float* r,
                  const float* w, const float* invDiag, float* out, int normalize, const int* skip,
-                 cudaStream_t s);
+                 cudaStream_t s, const NetUpdate* upd = nullptr);
 // NEKB_OK, or an error (and the flag cleared) when a tensor-core launch gave up
 // waiting for its input copies since the last call
 int net_tc_copy_timeout();
