@@ -382,20 +382,6 @@ __global__ void k_to_bf16(int P, const float* W, __nv_bfloat16* Wbf)
   if (p < P) Wbf[p] = __float2bfloat16_rn(W[p]);
 }
 
-// x += alpha p ; r -= alpha Ap (the FCG update, when the network runs on the CUDA cores)
-__global__ void k_net_update(int64_t N, const double* __restrict__ alpha, float* __restrict__ x,
-                             const float* __restrict__ p, const float* __restrict__ Ap,
-                             float* __restrict__ r, const int* skip)
-{
-  if (skip != nullptr && *skip != 0) return;
-  const float a = (float)*alpha;
-  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < N;
-       n += (int64_t)gridDim.x * blockDim.x) {
-    x[n] += a * p[n];
-    r[n] -= a * Ap[n];
-  }
-}
-
 // in = h r_e / s_e ; target = (e_e - invDiag r_e) / (h s_e), h = sqrt(invDiag) per node
 // (1 without invDiag), s_e = RMS of h r over element e
 __global__ void k_prepare_pairs(int Np, int64_t Efield, const float* __restrict__ r,
@@ -631,26 +617,14 @@ bool net_supported(int Nq, int C)
 
 }  // namespace
 
-int net_precondition(nekb_bp* bp, nekb_net* net, float* r, float* z, const float* invDiag,
-                     const float* w, const int* skip, cudaStream_t s, const NetUpdate* upd)
+int net_precondition(nekb_bp* bp, nekb_net* net, const float* r, float* z, const float* invDiag,
+                     const float* w, const int* skip, cudaStream_t s)
 {
   if (!net) return fail(NEKB_ERR_INVALID, "learned preconditioner: no network");
   if (net->Nq != bp->Nq) return fail(NEKB_ERR_INVALID, "net order Nq=%d differs from the mesh's %d", net->Nq, bp->Nq);
-  const int64_t Etot = bp->Nfields * bp->E;
-  const int mode = kNetNormalize | kNetAddJacobi;
   // z = w (h s net + invDiag r) per element copy, then assembled and masked
-  if (net->inference == NEKB_NET_TENSOR && net_tc_supported(net->Nq, net->C)) {
-    NEKB_TRY(net_infer_tc(net->Wbf.as<__nv_bfloat16>(), Etot, bp->E, r, w, invDiag, z, mode, skip,
-                          s, upd));
-  } else {
-    if (upd) {
-      const int64_t N = Etot * bp->Np;
-      const unsigned g = (unsigned)std::min<int64_t>((N + 255) / 256, 152 * 16);
-      k_net_update<<<g, 256, 0, s>>>(N, upd->alpha, upd->x, upd->p, upd->Ap, r, skip);
-      NEKB_CUDA(cudaGetLastError());
-    }
-    NEKB_TRY(net_infer(net, Etot, bp->E, r, w, invDiag, z, mode, skip, s));
-  }
+  NEKB_TRY(net_infer(net, bp->Nfields * bp->E, bp->E, r, w, invDiag, z,
+                     kNetNormalize | kNetAddJacobi, skip, s));
   NEKB_TRY(launch_gs_add(bp->ogs->Nmulti, bp->ogs->d_offsets, bp->ogs->d_ids, bp->Nfields,
                          bp->offset, z, NEKB_FLOAT, skip, s));
   NEKB_TRY(launch_mask(bp->Nmasked, bp->mask.as<int32_t>(), bp->Nfields, bp->offset, z, NEKB_FLOAT,

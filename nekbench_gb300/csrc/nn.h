@@ -7,22 +7,11 @@
 
 namespace nekb {
 
-// The Krylov update that precedes the preconditioner in an FCG iteration:
-// x += alpha p, r -= alpha Ap with alpha read from the device.
-struct NetUpdate {
-  const double* alpha;
-  float* x;
-  const float* p;
-  const float* Ap;
-};
-
 // z = Jacobi(r) + mask(gs(w * h * s_e * net(h * r_e / s_e))), h = sqrt(invDiag),
-// s_e = RMS of h * r over element e; with upd, r (and x) are first updated
-// (by the network kernel itself on the tensor-core path).
+// s_e = RMS of h * r over element e.
 // Runs on stream s; returns at once on the device when *skip != 0.
-int net_precondition(nekb_bp* bp, nekb_net* net, float* r, float* z, const float* invDiag,
-                     const float* w, const int* skip, cudaStream_t s,
-                     const NetUpdate* upd = nullptr);
+int net_precondition(nekb_bp* bp, nekb_net* net, const float* r, float* z, const float* invDiag,
+                     const float* w, const int* skip, cudaStream_t s);
 
 // inference mode bits: normalise by the element RMS of sqrt(invDiag) r; add
 // w invDiag r to the output
@@ -32,7 +21,7 @@ constexpr int kNetNormalize = 1, kNetAddJacobi = 2;
 bool net_tc_supported(int Nq, int C);
 int net_infer_tc(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const float* r,
                  const float* w, const float* invDiag, float* out, int normalize, const int* skip,
-                 cudaStream_t s, const NetUpdate* upd = nullptr);
+                 cudaStream_t s);
 // NEKB_OK, or an error (and the flag cleared) when a tensor-core launch gave up
 // waiting for its input copies since the last call
 int net_tc_copy_timeout();

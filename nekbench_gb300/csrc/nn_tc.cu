@@ -37,9 +37,8 @@ constexpr int kSmA0 = kSmZero + 32;                      // scaled input, 512 fl
 constexpr int kSmH = kSmA0 + kNp * 4;                    // sqrt(invDiag), 512 floats
 constexpr int kSmU = kSmH + kNp * 4;                     // [27][kUStride] floats
 constexpr int kSmRed = kSmU + kTaps * kUStride * 4;      // block-sum scratch
-constexpr int kRows = 6;                                 // r, invDiag, w, p, Ap, x
-constexpr int kSmIn = kSmRed + 64;                       // [2 buffers][kRows][512] floats
-constexpr int kSmBar = kSmIn + 2 * kRows * kNp * 4;      // two mbarriers
+constexpr int kSmIn = kSmRed + 64;                       // [2 buffers][r, invDiag, w][512] floats
+constexpr int kSmBar = kSmIn + 2 * 3 * kNp * 4;          // two mbarriers
 constexpr int kSmTotal = kSmBar + 16;
 constexpr int kRowBytes = kNp * 4;                       // one element row of a node array
 constexpr long kWaitLimit = 1L << 22;                    // bounded mbarrier waits
@@ -144,14 +143,11 @@ __device__ __forceinline__ float block_sum4(float v, float* red)
 
 __global__ void __launch_bounds__(kThreads, 2)
 k_net_infer_tc(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ Wbf,
-               float* __restrict__ r, const float* __restrict__ w,
+               const float* __restrict__ r, const float* __restrict__ w,
                const float* __restrict__ invDiag, float* __restrict__ out, int normalize,
-               const int* skip, NetUpdate upd)
+               const int* skip)
 {
   if (skip != nullptr && *skip != 0) return;
-  // with upd.x: x += alpha p and r -= alpha Ap for each element before it is used
-  const bool update = upd.x != nullptr;
-  const float alpha = update ? (float)*upd.alpha : 0.f;
   extern __shared__ __align__(128) unsigned char smem[];
   float* a0 = reinterpret_cast<float*>(smem + kSmA0);
   float* hs = reinterpret_cast<float*>(smem + kSmH);
@@ -199,11 +195,11 @@ k_net_infer_tc(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ W
   // this thread's accumulator rows: i = g, j = 2w (c0,c1) and 2w+1 (c2,c3)
   const int jA = 2 * warp, jB = 2 * warp + 1;
 
-  // input rows r, invDiag, w (and p, Ap, x) of an element: double-buffered in
-  // shared memory, filled by bulk copies that complete on the buffer's mbarrier
-  float* inb = reinterpret_cast<float*>(smem + kSmIn);
+  // input rows r, invDiag, w of an element: double-buffered in shared memory,
+  // filled by bulk copies that complete on the buffer's mbarrier
+  const float* inb = reinterpret_cast<const float*>(smem + kSmIn);
   const uint32_t in_s = smem_addr(smem + kSmIn), bar_s = smem_addr(smem + kSmBar);
-  const uint32_t nrows = 1u + (invDiag ? 1u : 0u) + (w ? 1u : 0u) + (update ? 3u : 0u);
+  const uint32_t nrows = 1u + (invDiag ? 1u : 0u) + (w ? 1u : 0u);
   if (tid == 0) {
     bar_init(bar_s);
     bar_init(bar_s + 8);
@@ -211,16 +207,11 @@ k_net_infer_tc(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ W
   }
   __syncthreads();
   auto fetch = [&](int64_t el, int buf) {  // one thread issues the copies of element el
-    const uint32_t bar = bar_s + 8 * buf, dst = in_s + buf * kRows * kRowBytes;
+    const uint32_t bar = bar_s + 8 * buf, dst = in_s + buf * 3 * kRowBytes;
     bar_expect(bar, nrows * kRowBytes);
     bulk_row(dst, r + el * kNp, bar);
     if (invDiag) bulk_row(dst + kRowBytes, invDiag + (el % Efield) * kNp, bar);
     if (w) bulk_row(dst + 2 * kRowBytes, w + (el % Efield) * kNp, bar);
-    if (update) {
-      bulk_row(dst + 3 * kRowBytes, upd.p + el * kNp, bar);
-      bulk_row(dst + 4 * kRowBytes, upd.Ap + el * kNp, bar);
-      bulk_row(dst + 5 * kRowBytes, upd.x + el * kNp, bar);
-    }
   };
   if (tid == 0 && (int64_t)blockIdx.x < Etot) fetch(blockIdx.x, 0);
   uint32_t parity0 = 0, parity1 = 0;
@@ -242,22 +233,9 @@ k_net_infer_tc(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ W
       }
       return;
     }
-    float* rin = inb + buf * kRows * kNp;
+    const float* rin = inb + buf * 3 * kNp;
     const float* din = rin + kNp;
     const float* win = rin + 2 * kNp;
-    if (update) {  // the FCG update of this element's rows; rin holds the new r
-      const float* pin = rin + 3 * kNp;
-      const float* apin = rin + 4 * kNp;
-      const float* xin = rin + 5 * kNp;
-#pragma unroll
-      for (int c = 0; c < kNp / kThreads; ++c) {
-        const int n = tid + c * kThreads;
-        const float rn = rin[n] - alpha * apin[n];
-        rin[n] = rn;
-        r[e * kNp + n] = rn;
-        upd.x[e * kNp + n] = xin[n] + alpha * pin[n];
-      }
-    }
     // ---- scaled input: a0 = h r / s
     float ss = 0.f;
 #pragma unroll
@@ -434,17 +412,12 @@ bool net_tc_supported(int Nq, int C) { return Nq == kNq && C == 16; }
 
 int net_infer_tc(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const float* r,
                  const float* w, const float* invDiag, float* out, int normalize, const int* skip,
-                 cudaStream_t s, const NetUpdate* upd)
+                 cudaStream_t s)
 {
   // the bulk copies move whole element rows: 16-byte aligned arrays
-  NetUpdate u{};
-  if (upd) u = *upd;
-  for (const void* p : {(const void*)r, (const void*)w, (const void*)invDiag, (const void*)u.x,
-                        (const void*)u.p, (const void*)u.Ap})
+  for (const void* p : {(const void*)r, (const void*)w, (const void*)invDiag})
     if (reinterpret_cast<uintptr_t>(p) % 16 != 0)
       return fail(NEKB_ERR_INVALID, "network: input arrays must be 16-byte aligned");
-  if (upd && (!u.alpha || !u.x || !u.p || !u.Ap))
-    return fail(NEKB_ERR_INVALID, "network: incomplete update arguments");
   static bool attr = false;
   if (!attr) {
     NEKB_CUDA(cudaFuncSetAttribute(k_net_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmTotal));
@@ -457,9 +430,8 @@ int net_infer_tc(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const f
   int64_t grid = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
   if (grid > Etot) grid = Etot;
   if (grid < 1) return NEKB_OK;
-  // r is written only with an update
-  k_net_infer_tc<<<(unsigned)grid, kThreads, kSmTotal, s>>>(Etot, Efield, Wbf, const_cast<float*>(r),
-                                                            w, invDiag, out, normalize, skip, u);
+  k_net_infer_tc<<<(unsigned)grid, kThreads, kSmTotal, s>>>(Etot, Efield, Wbf, r, w, invDiag, out,
+                                                            normalize, skip);
   NEKB_CUDA(cudaGetLastError());
   return NEKB_OK;
 }

@@ -673,10 +673,9 @@ int launch_fcg_iteration(const OpView& op, PcgArgs<T> a, const ExtPrecond* ext, 
       k_fcg_pap<T, 1><<<red_grid(a.Nloc), RT, 0, s>>>(a, ext->AP, Nall);
     }
     NEKB_CUDA(cudaGetLastError());
-    // x += alpha p, r -= alpha Ap inside the preconditioner's own pass
-    const NetUpdate upd{&a.st->alpha, a.x, a.p, a.Ap};
-    NEKB_TRY(net_precondition(ext->bp, ext->net, a.r, a.z, ext->invDiag, ext->w, &a.st->done, s,
-                              &upd));
+    k_update<T><<<vec_grid(Nall), RT, 0, s>>>(a);
+    NEKB_CUDA(cudaGetLastError());
+    NEKB_TRY(net_precondition(ext->bp, ext->net, a.r, a.z, ext->invDiag, ext->w, &a.st->done, s));
     return launch_fcg_dots<T, false>(a, ext, s);
   } else {
     return fail(NEKB_ERR_UNSUPPORTED, "FCG(m) runs in FP32 only");
