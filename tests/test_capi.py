@@ -92,3 +92,15 @@ def test_ogs_host_setup_matches_oracle_without_gpu_kernels():
     m = O.BoxMesh(3, 2, 2, 2)
     Ng, offs, gids, invdeg = O.ogs_setup(m.ids)
     assert offs[-1] == np.count_nonzero(m.ids) and Ng > 0
+
+
+def test_nekbone_summary_formulas_reproduce_the_published_run():
+    """The driver's throughput and flop figures follow nekBone/main.cpp:156-177:
+    fed the published V100 run (N=7, E=8192, BP5, 5000 iterations in 6.71864 s,
+    nekBone/readme.md:43-53) they give its 2.09109 GDOF/s/iter and 393.296
+    GFLOP/s."""
+    from nekbench_gb300.nekbone import throughput
+    gdofs, gbs, gflops = throughput(5000, 7, 8, 8192, 1, True, 6.71864)
+    assert abs(gdofs - 2.09109) < 1e-5
+    assert abs(gflops - 393.296) < 1e-3
+    assert gbs > 0
