@@ -21,8 +21,8 @@ def main(argv=None):
     p.add_argument("--n", type=int, default=24)
     p.add_argument("--train-seeds", type=int, default=200)
     p.add_argument("--eval-seeds", type=int, default=50)
-    p.add_argument("--steps", type=int, default=2000)
-    p.add_argument("--batch", type=int, default=2048)
+    p.add_argument("--steps", type=int, default=12000)
+    p.add_argument("--batch", type=int, default=4096)
     p.add_argument("--lr", type=float, default=2e-3)
     p.add_argument("--channels", type=int, default=16)
     p.add_argument("--frac", type=float, default=0.125)
