@@ -17,6 +17,11 @@
 //   K_upd : x += alpha p ; r -= alpha Ap ; z = M r ; (BPUpdatePCG fused with
 //           rdotz = sum w r z ; rdotr = sum w r r     BPPreconditioner and
 //           convergence test, beta                     BPWeightedInnerProduct2)
+// In the FP32 inner iterations K_pAp is replaced by the operator kernel's own
+// per-block sums of p . A_local p and a one-block reduction.  With the learned
+// preconditioner the iteration is truncated flexible CG, FCG(m): the new
+// direction is z minus its A-projections on the last m directions (ring
+// buffers), alpha = r.p / p.Ap.
 #include "bp.h"
 #include "nn.h"
 
