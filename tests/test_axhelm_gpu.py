@@ -228,3 +228,20 @@ def test_symmetry_and_linearity(nb, O, dev):
     assert abs(s1 - s2) / abs(s1) < 1e-12
     lin = (Auv - (2.0 * Au - 3.0 * Av)).abs().max() / Auv.abs().max()
     assert float(lin) < 1e-12
+
+
+@pytest.mark.parametrize("N,ndim,bk", [(3, 1, True), (7, 3, False), (9, 1, False)])
+def test_axhelm_driver(N, ndim, bk):
+    """The axhelm driver on the reference driver's inputs (Gauss D, random
+    ggeo and q): figures reported, double-float within 1e-12 and FP32 within
+    1e-5 (relative, max-norm) of the FP64 kernel."""
+    from nekbench_gb300 import axhelm_driver as drv
+    base = ["--N", str(N), "--E", "512", "--ndim", str(ndim), "--steps", "3", "--json"]
+    if bk:
+        base.append("--bk")
+    r64 = drv.main(base)
+    assert r64["gdofs"] > 0 and r64["gbs"] > 0 and r64["gflops"] > 0
+    rs = drv.main(base + ["--precision", "fp64_split"])
+    assert rs["max_rel_diff_to_fp64"] < 1e-12
+    r32 = drv.main(base + ["--precision", "fp32"])
+    assert r32["max_rel_diff_to_fp64"] < 1e-5
