@@ -1,7 +1,9 @@
 """axhelm benchmark driver on the GB300 library, after the reference's
 axhelm/main.cpp: one kernel variant and order on random inputs, timed over
 repetitions, reported as GDOF/s, GB/s and GFLOP/s with the reference's
-formulas (axhelm/main.cpp:161-169).
+formulas (axhelm/main.cpp:161-169), the bytes counted in the storage type of
+the precision (8-byte words for FP64 and double-float, 4 for FP32, 4-byte
+fields with 2-byte geometry and lambda for BF16 storage).
 
   python -m nekbench_gb300.axhelm_driver [--N 7] [--E 262144] [--ndim 1] [--bk]
       [--precision fp64|fp64_split|fp32|bf16] [--steps 100] [--json]
@@ -36,12 +38,12 @@ def parse(argv=None):
     return p.parse_args(argv)
 
 
-def figures(N, E, ndim, bk, seconds):
+def figures(N, E, ndim, bk, seconds, word_field=WORD, word_geom=WORD):
     """GDOF/s, GB/s, GFLOP/s of one application (axhelm/main.cpp:161-169)."""
     Nq = N + 1
     Np = Nq ** 3
     gdofs = ndim * N ** 3 * E / seconds / 1e9
-    bytes_el = (ndim * 2 * Np + 7 * Np + (0 if bk else 2 * Np)) * WORD
+    bytes_el = ndim * 2 * Np * word_field + (7 * Np + (0 if bk else 2 * Np)) * word_geom
     flops_el = ndim * (Np * 12 * Nq + 15 * Np + (0 if bk else 5 * Np))
     return gdofs, bytes_el * E / seconds / 1e9, flops_el * E / seconds / 1e9
 
@@ -91,7 +93,8 @@ def main(argv=None):
     e1.record()
     torch.cuda.synchronize()
     sec = e0.elapsed_time(e1) * 1e-3 / a.steps
-    gdofs, gbs, gflops = figures(N, E, nd, a.bk, sec)
+    wf, wg = {nb.FP64: (8, 8), nb.FP64_SPLIT: (8, 8), nb.FP32: (4, 4), nb.BF16: (4, 2)}[prec]
+    gdofs, gbs, gflops = figures(N, E, nd, a.bk, sec, wf, wg)
     res = {"N": N, "Nelements": E, "Ndim": nd, "bk": a.bk, "precision": a.precision,
            "repetitions": a.steps, "ms": sec * 1e3, "gdofs": gdofs, "gbs": gbs, "gflops": gflops}
     if prec != nb.FP64:
