@@ -70,7 +70,8 @@ int nekb_copy(void* dst, const void* src, int64_t bytes);
  *   kernel(Nelements, offset, o_ggeo, o_D, o_lambda, o_q, o_Aq)
  * (nekBone/solve.cpp:218, axhelm/main.cpp:132) and, with NEKB_AX_PARTIAL,
  *   kernel(Nelements, offset, o_elementList, o_ggeo, o_D, o_lambda, o_q, o_Aq)
- * (nekBone/solve.cpp:192-200).  Nq = N+1 in [2, 12].  lambda may be NULL in BK
+ * (nekBone/solve.cpp:192-200).  Nq = N+1 in [2, 14] for NEKB_FP64 and [2, 12]
+ * for the other precisions.  lambda may be NULL in BK
  * mode.  D is double for NEKB_FP64 and float otherwise.  All pointers are
  * device pointers. */
 int nekb_axhelm(int Nq, int flags, int precision, int64_t Nelements, int64_t offset,

@@ -88,7 +88,7 @@ int nekb_axhelm(int Nq, int flags, int precision, int64_t Nelements, int64_t off
   if ((flags & NEKB_AX_PARTIAL) && !elementList)
     return fail(NEKB_ERR_INVALID, "axhelm: Partial variant needs an element list");
   if (!(flags & NEKB_AX_BK) && !lambda) return fail(NEKB_ERR_INVALID, "axhelm: lambda is NULL outside BK mode");
-  if (Nq < kMinNq || Nq > kMaxNq) return fail(NEKB_ERR_UNSUPPORTED, "axhelm: Nq=%d outside 2..12", Nq);
+  if (Nq < kMinNq || Nq > kMaxNq) return fail(NEKB_ERR_UNSUPPORTED, "axhelm: Nq=%d outside 2..%d", Nq, kMaxNq);
   const int64_t Np = (int64_t)Nq * Nq * Nq;
   const int64_t nf = (flags & NEKB_AX_N3) ? 3 : 1;
   if (!(flags & NEKB_AX_PARTIAL) && offset < Nelements * Np)

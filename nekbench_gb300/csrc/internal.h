@@ -28,7 +28,8 @@ void clear_error();
     if (nekb_s_ != NEKB_OK) return nekb_s_; \
   } while (0)
 
-constexpr int kMaxNq = 12;
+constexpr int kMaxNq = 14;      // FP64; the other precisions go to kMaxNqReduced
+constexpr int kMaxNqReduced = 12;
 constexpr int kMinNq = 2;
 
 // ---------------------------------------------------------------- basis (host)

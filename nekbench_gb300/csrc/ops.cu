@@ -21,6 +21,8 @@ namespace nekb {
   int launch_axhelm_##P##_nq11(int, const AxArgs&, cudaStream_t);           \
   int launch_axhelm_##P##_nq12(int, const AxArgs&, cudaStream_t);
 NEKB_DECL_AX(f64)
+int launch_axhelm_f64_nq13(int, const AxArgs&, cudaStream_t);
+int launch_axhelm_f64_nq14(int, const AxArgs&, cudaStream_t);
 NEKB_DECL_AX(f32)
 NEKB_DECL_AX(bf16)
 NEKB_DECL_AX(tri)
@@ -44,9 +46,14 @@ NEKB_DECL_AX(x)
 
 int launch_axhelm(int Nq, int flags, int precision, const AxArgs& a, cudaStream_t s)
 {
-  if (Nq < kMinNq || Nq > kMaxNq) return fail(NEKB_ERR_UNSUPPORTED, "axhelm: Nq=%d outside 2..12", Nq);
+  if (Nq < kMinNq || Nq > kMaxNq) return fail(NEKB_ERR_UNSUPPORTED, "axhelm: Nq=%d outside 2..%d", Nq, kMaxNq);
   if (flags & ~(NEKB_AX_BK | NEKB_AX_N3 | NEKB_AX_PARTIAL))
     return fail(NEKB_ERR_INVALID, "axhelm: unknown flag bits 0x%x", flags);
+  if (precision != NEKB_FP64 && Nq > kMaxNqReduced)
+    return fail(NEKB_ERR_UNSUPPORTED, "axhelm: Nq=%d is built for FP64 only (other precisions: Nq <= %d)",
+                Nq, kMaxNqReduced);
+  if (precision == NEKB_FP64 && Nq == 13) return launch_axhelm_f64_nq13(flags, a, s);
+  if (precision == NEKB_FP64 && Nq == 14) return launch_axhelm_f64_nq14(flags, a, s);
   switch (precision) {
     case NEKB_FP64: NEKB_SWITCH_AX(f64)
     case NEKB_FP32: NEKB_SWITCH_AX(f32)

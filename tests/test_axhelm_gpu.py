@@ -35,9 +35,16 @@ def fields(O, L, nf, seed):
 
 
 @pytest.mark.parametrize("prec", ["FP64", "FP64_SPLIT"])
-@pytest.mark.parametrize("N", list(range(1, 12)))
+@pytest.mark.parametrize("N", list(range(1, 14)))
 @pytest.mark.parametrize("flags", [0, 1, 2, 3])
 def test_fp64_all_orders_variants(nb, O, dev, N, flags, prec):
+    if prec != "FP64" and N > 11:
+        with pytest.raises(nb.NekbError):
+            nb.axhelm(N + 1, flags, getattr(nb, prec), 1, (N + 1) ** 3,
+                      *(torch.zeros(n, dtype=torch.float64, device=dev) for n in
+                        (7 * (N + 1) ** 3, (N + 1) ** 2, 2 * (N + 1) ** 3, 3 * (N + 1) ** 3,
+                         3 * (N + 1) ** 3)))
+        return
     m = O.BoxMesh(N, 3, 2, 2, perturb=0.1, seed=N)  # E=12, not a multiple of the CTA's elements
     E, L = m.E, m.Nlocal
     nf = 3 if flags & nb.AX_N3 else 1

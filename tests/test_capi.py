@@ -64,7 +64,9 @@ def test_host_basis_matches_oracle(N):
 def test_argument_errors_without_a_launch():
     L = nb.lib()
     # order outside the built range: rejected before any device work
-    rc = L.nekb_axhelm(13, 0, nb.FP64, 1, 13 ** 3, None, 1, 1, 1, 1, 1, None)
+    rc = L.nekb_axhelm(15, 0, nb.FP64, 1, 15 ** 3, None, 1, 1, 1, 1, 1, None)
+    assert rc == nb.ERR_UNSUPPORTED
+    rc = L.nekb_axhelm(13, 0, nb.FP32, 1, 13 ** 3, None, 1, 1, 1, 1, 1, None)  # FP64 only there
     assert rc == nb.ERR_UNSUPPORTED
     rc = L.nekb_axhelm(8, 0, nb.FP64, -1, 0, None, 1, 1, 1, 1, 1, None)
     assert rc == nb.ERR_INVALID
