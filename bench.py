@@ -408,6 +408,69 @@ def nekbone_bp5(nb, torch, dev):
     return out
 
 
+def dot_adv(nb, torch, dev, E, peak_bw, fp64_peak):
+    """The dot and adv benchmark kernels at N=7.  dot: weightedInnerProduct2_v0
+    partials over E elements (3 arrays of E*512 doubles, larger than L2) timed
+    alone (CUDA events) and as the reference driver times a call (kernel, copy
+    of the partials to the host, host sum; dot/main.cpp:27-48).  adv:
+    advCubatureHex3D_v0 with cubN=11 on 8192 elements, FP64-pipe bound."""
+    from nekbench_gb300 import adv as advmod
+    out = {}
+    L = E * 512
+    arrs = [torch.empty(L, dtype=torch.float64, device=dev) for _ in range(3)]
+    for s, t in enumerate(arrs):
+        nb.fill_uniform(t, 1, 10 + s, 0.0, 1.0)
+    nblk = nb.dot_num_blocks(L)
+    tmp = torch.empty(nblk, dtype=torch.float64, device=dev)
+    host = torch.empty(nblk, dtype=torch.float64, pin_memory=True)
+    for _ in range(3):
+        nb.dot_partials(0, L, *arrs, tmp)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(20):
+        nb.dot_partials(0, L, *arrs, tmp)
+    e1.record()
+    torch.cuda.synchronize()
+    kern = e0.elapsed_time(e1) * 1e-3 / 20
+    t0 = time.perf_counter()
+    for _ in range(10):
+        nb.dot_partials(0, L, *arrs, tmp)
+        host.copy_(tmp)
+        float(np.cumsum(host.numpy())[-1])
+    call = (time.perf_counter() - t0) / 10
+    out["dot"] = {"workload": f"weightedInnerProduct2_v0, N=7, E={E} ({L} nodes), blockSize 256",
+                  "kernel_ms": kern * 1e3, "kernel_gbs": 24 * L / kern / 1e9,
+                  "hbm_frac": 24 * L / kern / 1e9 / peak_bw,
+                  "reference_call_ms": call * 1e3, "reference_call_gbs": 24 * L / call / 1e9,
+                  "gdofs": E * 343 / kern / 1e9}
+    del arrs, tmp, host
+    Nq, cq, Ea = 8, 12, 8192
+    g = torch.Generator(device=dev).manual_seed(5)
+    r = lambda n: torch.rand(n, dtype=torch.float64, device=dev, generator=g)  # noqa: E731
+    vgeo, cub, D, I, U = r(12 * Ea * 512), r(12 * Ea * cq ** 3), r(cq * cq), r(Nq * cq), r(3 * Ea * 512)
+    NU = torch.empty_like(U)
+    for _ in range(3):
+        nb.adv_cubature(Nq, cq, Ea, vgeo, cub, D, I, Ea * 512, U, NU)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(5):
+        nb.adv_cubature(Nq, cq, Ea, vgeo, cub, D, I, Ea * 512, U, NU)
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) * 1e-3 / 5
+    tflops = advmod.flops(Nq, cq) * Ea / t / 1e12
+    out["adv"] = {"workload": "advCubatureHex3D_v0, N=7, cubN=11, E=8192, FP64",
+                  "ms": t * 1e3, "gdofs": Ea * 343 / t / 1e9, "fp64_tflops": tflops,
+                  "fp64_peak_tflops_measured": fp64_peak, "fp64_frac": tflops / fp64_peak,
+                  "gbs": advmod.bytes_moved(Nq, cq) * Ea / t / 1e9,
+                  "flops_per_element": advmod.flops(Nq, cq),
+                  "bytes_per_element": advmod.bytes_moved(Nq, cq)}
+    del vgeo, cub, U, NU
+    torch.cuda.empty_cache()
+    return out
+
+
 def learned_net(nb, torch, dev):
     path = os.path.join(ROOT, "nekbench_gb300", "weights", "precond_n7_c16.bin")
     if not os.path.exists(path) or not hasattr(nb, "Net"):
@@ -527,6 +590,8 @@ def run_gpu(args, rank, ws, local):
         v["bf16_peak_tflops"] = measured_bf16()
         v["frac_of_bf16_peak"] = v["tflops"] / v["bf16_peak_tflops"]
 
+    benchmarks = dot_adv(nb, torch, dev, E, peak_bw, fp64_peak)
+
     cpu = CpuAxhelm().rate(args.cpu_seconds) if (rank == 0 and ws == 1) else None
     if rank != 0:
         return
@@ -556,6 +621,7 @@ def run_gpu(args, rank, ws, local):
         "pcg": pcg,
         "nekbone_bp5": bp5,
         "learned_preconditioner_inference": net_cost,
+        "dot_and_adv_benchmarks": benchmarks,
         "reference_published": {"v100_axhelm_gdofs": V100_PUBLISHED_GDOFS},
     }
     print(json.dumps(line), flush=True)

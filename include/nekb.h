@@ -269,6 +269,45 @@ int nekb_weighted_inner_product_noalloc(int64_t N, int Nfields, int64_t offset, 
                                         const double* a, const double* b, double* wab,
                                         void* stream);
 
+/* ------------------------------------------------------------------ dot benchmark */
+/* The dot benchmark's kernels (dot/kernel/VOLTA/dot.okl), launched by the
+ * driver as kernel(N, o_w, o_x, o_y, o_tmp) (dot/main.cpp:27-48, 123-126):
+ * wxy[b] (device, nekb_dot_num_blocks(N, blockSize) doubles) = the sum over
+ * block b of blockSize consecutive nodes, reduced in the reference kernel's
+ * own tree, so every partial is bit-for-bit the reference's; the caller sums
+ * the partials (the driver does it on the host in block order).
+ *   variant 0: weightedInnerProduct2_v0 (dot.okl:27-65), w[i] x[i] y[i],
+ *              blockSize = p_blockSize (256, 512 or 1024);
+ *   variant 1: weightedInnerProduct2_v1 (dot.okl:114-169), blocks of 256
+ *              nodes reduced as 8 groups of 32 (the lockstep tree);
+ *   variant 2: weightedBlockInnerProduct2 (dot.okl:67-111), per node the sum
+ *              over Nfields (p_eNfields, 1..3) of w x y at i + f*offset.
+ * N = 0 writes nothing.  Asynchronous on the stream. */
+int64_t nekb_dot_num_blocks(int64_t N, int blockSize);
+int nekb_dot_partials(int variant, int64_t N, int Nfields, int64_t offset, int blockSize,
+                      const double* w, const double* x, const double* y, double* wxy,
+                      void* stream);
+
+/* ------------------------------------------------------------------ adv benchmark */
+/* advCubatureHex3D_v0 (adv/kernel/VOLTA/adv.okl:27-261), launched as
+ * kernel(Nelements, o_vgeo, o_cubvgeo, o_cubD, o_cubInterpT, offset, o_U, o_NU)
+ * (adv/main.cpp:115-123), FP64: the dealiased advection term of the velocity
+ * U (3 fields, field f at U + f*offset, node i + Nq j + Nq^2 k of element e at
+ * e*Nq^3 + ...):
+ *   NU_f = IJW . (I^T x I^T x I^T) [Uhat dUc_f/dr + Vhat dUc_f/ds + What dUc_f/dt],
+ *   Uc = (I x I x I) U,  Uhat = JW (Uc . grad r), Vhat = JW (Uc . grad s), What = JW (Uc . grad t)
+ * with I(i <- a) = cubInterpT[a*cubNq + i] (Nq x cubNq), the cubature
+ * derivative cubD[i*cubNq + n] (cubNq x cubNq), the metric slots RX..TZ and JW
+ * of cubvgeo (12 slots of cubNq^3 per element) and IJW of vgeo (12 slots of
+ * Nq^3), slot numbers of core/params.h:2-13.  Built for cubNq = Nq (Nq 2..12)
+ * and cubNq = ceil(3 Nq / 2) (Nq 2..10); NEKB_ERR_UNSUPPORTED otherwise.
+ * For cubNq > Nq the reference kernel indexes its Nq x Nq shared tile s_U with
+ * cubNq x cubNq indices (adv.okl:203-231); this operator uses a cubNq x cubNq
+ * slice there (the two agree for cubNq = Nq).  Asynchronous on the stream. */
+int nekb_adv_cubature(int Nq, int cubNq, int64_t Nelements, const double* vgeo,
+                      const double* cubvgeo, const double* cubD, const double* cubInterpT,
+                      int64_t offset, const double* U, double* NU, void* stream);
+
 void nekb_pcg_default_opts(nekb_pcg_opts* opts);
 int nekb_bp_pcg(nekb_bp* bp, const double* lambda, double* r, double* x, double tol, int maxit,
                 const nekb_pcg_opts* opts, nekb_pcg_stats* stats);

@@ -47,6 +47,7 @@ EXPORTED = [
     "nekb_net_num_params", "nekb_net_get_weights",
     "nekb_net_set_weights", "nekb_net_forward", "nekb_net_train_step", "nekb_net_gradient",
     "nekb_net_prepare_pairs", "nekb_net_save", "nekb_net_load", "nekb_peak_fma", "nekb_peak_copy",
+    "nekb_dot_num_blocks", "nekb_dot_partials", "nekb_adv_cubature",
 ]
 
 
@@ -129,6 +130,10 @@ def lib():
     L.nekb_pcg_default_opts.argtypes = [C.POINTER(PcgOpts)]
     L.nekb_bp_pcg.argtypes = [vp, vp, vp, vp, d, i32, C.POINTER(PcgOpts), C.POINTER(PcgStats)]
     L.nekb_bp_zero_mean.argtypes = [vp, vp]
+    L.nekb_dot_num_blocks.restype = i64
+    L.nekb_dot_num_blocks.argtypes = [i64, i32]
+    L.nekb_dot_partials.argtypes = [i32, i64, i32, i64, i32, vp, vp, vp, vp, vp]
+    L.nekb_adv_cubature.argtypes = [i32, i32, i64, vp, vp, vp, vp, i64, vp, vp, vp]
     if hasattr(L, "nekb_net_create"):
         L.nekb_net_create.restype = vp
         L.nekb_net_create.argtypes = [i32, i32, i32, C.c_uint64, C.POINTER(C.c_int)]
@@ -543,6 +548,58 @@ class Net:
 def prepare_pairs(Np, E, Efield, r, err, inv_diag, inp, target, stream=None):
     check(lib().nekb_net_prepare_pairs(Np, E, Efield, _ptr(r), _ptr(err), _ptr(inv_diag),
                                        _ptr(inp), _ptr(target), _stream(stream)))
+
+
+# --------------------------------------------------------------------------- dot, adv
+DOT_V0, DOT_V1, DOT_BLOCK = 0, 1, 2
+_DOT_NAMES = {"weightedInnerProduct2_v0": DOT_V0, "weightedInnerProduct2_v1": DOT_V1,
+              "weightedBlockInnerProduct2": DOT_BLOCK}
+
+
+def dot_num_blocks(N, block_size=256):
+    return check_value(lib().nekb_dot_num_blocks(N, block_size))
+
+
+def dot_partials(variant, N, w, x, y, wxy, Nfields=1, offset=0, block_size=256, stream=None):
+    """Per-block partials of the dot benchmark kernels (dot/kernel/VOLTA/dot.okl)."""
+    _require_cuda(w, x, y, wxy)
+    check(lib().nekb_dot_partials(variant, N, Nfields, offset, block_size, _ptr(w), _ptr(x), _ptr(y),
+                                  _ptr(wxy), _stream(stream)))
+
+
+def load_dot_kernel(name: str, block_size: int = 256, Nfields: int = 1):
+    """Kernel object with the argument order of the dot driver's kernel
+    (dot/main.cpp:31): ``kernel(N, w, x, y, wxy)``; weightedBlockInnerProduct2
+    takes ``kernel(N, offset, w, x, y, wxy)`` (dot.okl:67)."""
+    if name not in _DOT_NAMES:
+        raise NekbError(ERR_INVALID, f"unknown dot kernel {name!r}")
+    variant = _DOT_NAMES[name]
+    if variant == DOT_BLOCK:
+        def kernel(N, offset, w, x, y, wxy):
+            dot_partials(variant, N, w, x, y, wxy, Nfields, offset, block_size)
+    else:
+        def kernel(N, w, x, y, wxy):
+            dot_partials(variant, N, w, x, y, wxy, 1, 0, block_size)
+    kernel.variant, kernel.block_size, kernel.name = variant, block_size, name
+    return kernel
+
+
+def adv_cubature(Nq, cubNq, Nelements, vgeo, cubvgeo, cubD, cubInterpT, offset, U, NU, stream=None):
+    """advCubatureHex3D_v0 (adv/kernel/VOLTA/adv.okl:27) on device tensors."""
+    _require_cuda(vgeo, cubvgeo, cubD, cubInterpT, U, NU)
+    check(lib().nekb_adv_cubature(Nq, cubNq, Nelements, _ptr(vgeo), _ptr(cubvgeo), _ptr(cubD),
+                                  _ptr(cubInterpT), offset, _ptr(U), _ptr(NU), _stream(stream)))
+
+
+def load_adv_kernel(N: int, cubN: int):
+    """Kernel object with the adv driver's argument order (adv/main.cpp:115-123):
+    ``kernel(Nelements, vgeo, cubvgeo, cubD, cubInterpT, offset, U, NU)``."""
+    Nq, cubNq = N + 1, cubN + 1
+
+    def kernel(Nelements, vgeo, cubvgeo, cubD, cubInterpT, offset, U, NU):
+        adv_cubature(Nq, cubNq, Nelements, vgeo, cubvgeo, cubD, cubInterpT, offset, U, NU)
+    kernel.Nq, kernel.cubNq, kernel.name = Nq, cubNq, "advCubatureHex3D_v0"
+    return kernel
 
 
 def peak_fma(fp64=True):

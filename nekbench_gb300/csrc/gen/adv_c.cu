@@ -1,0 +1,13 @@
+// Instantiations of the adv operator kernel (adv_impl.cuh) for (Nq, cubNq) = (10, 10), (7, 11), (8, 12).
+#include "adv_impl.cuh"
+
+namespace nekb {
+namespace adv {
+template int launch<10, 10>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+                            const double*, double*, cudaStream_t);
+template int launch<7, 11>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+                            const double*, double*, cudaStream_t);
+template int launch<8, 12>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+                            const double*, double*, cudaStream_t);
+}  // namespace adv
+}  // namespace nekb

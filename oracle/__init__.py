@@ -74,6 +74,9 @@ def lib():
     L.nekbo_conv3d_backward.argtypes = [C.c_int, C.c_int64, C.c_int, C.c_int, _f, _f, _f, _vp, _f]
     L.nekbo_gelu_forward.argtypes = [C.c_int64, _f, _f]
     L.nekbo_gelu_backward.argtypes = [C.c_int64, _f, _f, _f]
+    L.nekbo_dot_partials.restype = C.c_int64
+    L.nekbo_dot_partials.argtypes = [C.c_int, C.c_int64, C.c_int, C.c_int64, C.c_int, _d, _d, _d, _d]
+    L.nekbo_adv_cubature.argtypes = [C.c_int, C.c_int, C.c_int64, _d, _d, _d, _d, C.c_int64, _d, _d]
     _LIB = L
     return L
 
@@ -233,6 +236,27 @@ def zero_mean(q, Nloc, Nfields=1, offset=None):
     offset = Nloc if offset is None else offset
     lib().nekbo_zero_mean(Nloc, Nfields, offset, q)
     return q
+
+
+# ----------------------------------------------------------------------------- dot, adv
+def dot_partials(variant, w, x, y, N=None, Nfields=1, offset=0, block_size=256):
+    """Per-block partials of the dot benchmark kernels (dot/kernel/VOLTA/dot.okl)."""
+    N = w.size if N is None and Nfields == 1 else N
+    out = np.zeros(max(1, -(-N // block_size)), dtype=np.float64)
+    nb = lib().nekbo_dot_partials(variant, N, Nfields, offset, block_size,
+                                  *(np.ascontiguousarray(a, np.float64) for a in (w, x, y)), out)
+    if nb < 0:
+        raise ValueError("dot: bad arguments")
+    return out[:nb]
+
+
+def adv_cubature(Nq, cubNq, E, vgeo, cubvgeo, cubD, cubInterpT, U, offset=None):
+    """advCubatureHex3D_v0 restatement (adv/kernel/VOLTA/adv.okl:27-261)."""
+    offset = E * Nq ** 3 if offset is None else offset
+    NU = np.zeros(3 * offset, dtype=np.float64)
+    args = [np.ascontiguousarray(a, np.float64) for a in (vgeo, cubvgeo, cubD, cubInterpT)]
+    lib().nekbo_adv_cubature(Nq, cubNq, E, *args, offset, np.ascontiguousarray(U, np.float64), NU)
+    return NU
 
 
 # ----------------------------------------------------------------------------- conv net

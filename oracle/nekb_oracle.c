@@ -794,3 +794,144 @@ void nekbo_gelu_backward(int64_t n, const float* x, const float* gy, float* gx)
     gx[i] = (float)(gy[i] * d);
   }
 }
+
+/* ---- dot benchmark: dot/kernel/VOLTA/dot.okl:27-169 ----
+ * Each block fills s[t] (the weighted triple product of node b*B + t, 0 past
+ * N; dot.okl:36-39, 77-85, 128-137), then halves it in place: s[t] += s[t+h]
+ * for t < h.  Every step writes only below h and reads only at h or above, so
+ * running the threads of a step one after the other is the same as running
+ * them together. */
+int64_t nekbo_dot_partials(int variant, int64_t N, int Nfields, int64_t offset, int blockSize,
+                           const double* w, const double* x, const double* y, double* wxy)
+{
+  if (variant < 0 || variant > 2 || N < 0) return -1;
+  if (blockSize != 256 && blockSize != 512 && blockSize != 1024) return -1;
+  if (variant == 1 && blockSize != 256) return -1;
+  const int NF = variant == 2 ? Nfields : 1;
+  if (NF < 1 || NF > 3 || (NF > 1 && offset < N)) return -1;
+  const int B = blockSize;
+  const int64_t nblock = (N + B - 1) / B;
+  double s[1024];
+  for (int64_t b = 0; b < nblock; ++b) {
+    for (int t = 0; t < B; ++t) {
+      const int64_t id = t + (int64_t)B * b;
+      if (variant == 2) { /* dot.okl:79-84 */
+        double res = 0.0;
+        if (id < N)
+          for (int f = 0; f < NF; ++f) res += w[id + f * offset] * x[id + f * offset] * y[id + f * offset];
+        s[t] = res;
+      } else {
+        s[t] = id < N ? w[id] * x[id] * y[id] : 0.0;
+      }
+    }
+    if (variant == 1) { /* dot.okl:141-167: 8 groups of 32, then the group sums */
+      double sb[8];
+      for (int g = 0; g < 8; ++g) {
+        double* a = s + 32 * g;
+        for (int h = 16; h >= 2; h >>= 1)
+          for (int t = 0; t < h; ++t) a[t] += a[t + h];
+        sb[g] = a[0] + a[1];
+      }
+      for (int h = 4; h >= 1; h >>= 1)
+        for (int t = 0; t < h; ++t) sb[t] += sb[t + h];
+      wxy[b] = sb[0];
+    } else { /* dot.okl:41-63 */
+      for (int h = B / 2; h >= 2; h >>= 1)
+        for (int t = 0; t < h; ++t) s[t] += s[t + h];
+      wxy[b] = s[0] + s[1];
+    }
+  }
+  return nblock;
+}
+
+/* ---- adv benchmark: advCubatureHex3D_v0, adv/kernel/VOLTA/adv.okl:27-261 ----
+ * Same loop structure as the kernel: for each GLL plane c the r and s
+ * interpolations (adv.okl:86-115) and the progressive t accumulation
+ * (:117-123); derivatives and the advection term per cubature node
+ * (:133-197); then per GLL plane c the t, s and r projections and the inverse
+ * mass (:199-259). */
+void nekbo_adv_cubature(int Nq, int cubNq, int64_t Nelements, const double* vgeo,
+                        const double* cubvgeo, const double* cubD, const double* cubInterpT,
+                        int64_t offset, const double* U, double* NU)
+{
+  enum { RX = 0, RY = 1, SX = 2, SY = 3, JW = 5, IJW = 6, RZ = 7, SZ = 8, TX = 9, TY = 10, TZ = 11, NV = 12 };
+  const int Np = Nq * Nq * Nq, cq = cubNq, cNp = cq * cq * cq;
+  double* Uc = (double*)malloc(sizeof(double) * 3 * cNp);
+  double* A = (double*)malloc(sizeof(double) * 3 * cNp);
+  double* T1 = (double*)malloc(sizeof(double) * 3 * Nq * cq);
+  double* P1 = (double*)malloc(sizeof(double) * 3 * cq * cq);
+#define I_(a, i) cubInterpT[(a) * cq + (i)]
+#define D_(i, n) cubD[(i) * cq + (n)]
+  for (int64_t e = 0; e < Nelements; ++e) {
+    for (int n = 0; n < 3 * cNp; ++n) Uc[n] = 0.0;
+    for (int c = 0; c < Nq; ++c) {
+      for (int f = 0; f < 3; ++f)
+        for (int b = 0; b < Nq; ++b)
+          for (int i = 0; i < cq; ++i) {
+            double acc = 0.0;
+            for (int a = 0; a < Nq; ++a) acc += I_(a, i) * U[f * offset + e * Np + c * Nq * Nq + b * Nq + a];
+            T1[(f * Nq + b) * cq + i] = acc;
+          }
+      for (int f = 0; f < 3; ++f)
+        for (int j = 0; j < cq; ++j)
+          for (int i = 0; i < cq; ++i) {
+            double u2 = 0.0;
+            for (int b = 0; b < Nq; ++b) u2 += I_(b, j) * T1[(f * Nq + b) * cq + i];
+            for (int k = 0; k < cq; ++k) Uc[f * cNp + (k * cq + j) * cq + i] += I_(c, k) * u2;
+          }
+    }
+    for (int k = 0; k < cq; ++k)
+      for (int j = 0; j < cq; ++j)
+        for (int i = 0; i < cq; ++i) {
+          double dr[3], ds[3], dt[3];
+          for (int f = 0; f < 3; ++f) {
+            const double* u = Uc + f * cNp;
+            double ar = 0.0, as = 0.0, at = 0.0;
+            for (int n = 0; n < cq; ++n) ar += D_(i, n) * u[(k * cq + j) * cq + n];
+            for (int n = 0; n < cq; ++n) as += D_(j, n) * u[(k * cq + n) * cq + i];
+            for (int n = 0; n < cq; ++n) at += D_(k, n) * u[(n * cq + j) * cq + i];
+            dr[f] = ar;
+            ds[f] = as;
+            dt[f] = at;
+          }
+          const int64_t g = e * (int64_t)cNp * NV + (k * cq + j) * cq + i;
+          const int node = (k * cq + j) * cq + i;
+          const double un = Uc[node], vn = Uc[cNp + node], wn = Uc[2 * cNp + node];
+          const double jw = cubvgeo[g + JW * cNp];
+          const double Uhat = jw * (un * cubvgeo[g + RX * cNp] + vn * cubvgeo[g + RY * cNp] + wn * cubvgeo[g + RZ * cNp]);
+          const double Vhat = jw * (un * cubvgeo[g + SX * cNp] + vn * cubvgeo[g + SY * cNp] + wn * cubvgeo[g + SZ * cNp]);
+          const double What = jw * (un * cubvgeo[g + TX * cNp] + vn * cubvgeo[g + TY * cNp] + wn * cubvgeo[g + TZ * cNp]);
+          for (int f = 0; f < 3; ++f) A[f * cNp + node] = Uhat * dr[f] + Vhat * ds[f] + What * dt[f];
+        }
+    for (int c = 0; c < Nq; ++c) {
+      for (int f = 0; f < 3; ++f)
+        for (int j = 0; j < cq; ++j)
+          for (int i = 0; i < cq; ++i) {
+            double acc = 0.0;
+            for (int k = 0; k < cq; ++k) acc += I_(c, k) * A[f * cNp + (k * cq + j) * cq + i];
+            P1[(f * cq + j) * cq + i] = acc;
+          }
+      for (int f = 0; f < 3; ++f)
+        for (int b = 0; b < Nq; ++b)
+          for (int i = 0; i < cq; ++i) {
+            double acc = 0.0;
+            for (int j = 0; j < cq; ++j) acc += I_(b, j) * P1[(f * cq + j) * cq + i];
+            T1[(f * Nq + b) * cq + i] = acc;
+          }
+      for (int f = 0; f < 3; ++f)
+        for (int b = 0; b < Nq; ++b)
+          for (int a = 0; a < Nq; ++a) {
+            double acc = 0.0;
+            for (int i = 0; i < cq; ++i) acc += I_(a, i) * T1[(f * Nq + b) * cq + i];
+            const int m = c * Nq * Nq + b * Nq + a;
+            NU[f * offset + e * Np + m] = vgeo[e * (int64_t)Np * NV + IJW * Np + m] * acc;
+          }
+    }
+  }
+#undef I_
+#undef D_
+  free(Uc);
+  free(A);
+  free(T1);
+  free(P1);
+}

@@ -112,6 +112,28 @@ void nekbo_conv3d_backward(int Nq, int64_t Nelem, int Cin, int Cout, const float
 void nekbo_gelu_forward(int64_t n, const float* x, float* y);
 void nekbo_gelu_backward(int64_t n, const float* x, const float* gy, float* gx);
 
+/* ---- dot benchmark (dot/kernel/VOLTA/dot.okl) ----
+ * Per-block partials wxy[b] of blockSize consecutive nodes, reduced in the
+ * kernels' tree: variant 0 weightedInnerProduct2_v0 (dot.okl:27-65), 1
+ * weightedInnerProduct2_v1 (dot.okl:114-169, its lockstep tree), 2
+ * weightedBlockInnerProduct2 (dot.okl:67-111, Nfields triple products per
+ * node).  Returns the number of blocks written, or -1 on bad arguments.
+ * Parity unpinned: the kernels exist only as OKL (the OCCA runtime they need
+ * builds only with CMake), so this is a restatement checked by its own tests. */
+int64_t nekbo_dot_partials(int variant, int64_t N, int Nfields, int64_t offset, int blockSize,
+                           const double* w, const double* x, const double* y, double* wxy);
+
+/* ---- adv benchmark: advCubatureHex3D_v0 (adv/kernel/VOLTA/adv.okl:27-261) ----
+ * NU_f = IJW . (I^T x I^T x I^T)[Uhat dUc_f/dr + Vhat dUc_f/ds + What dUc_f/dt],
+ * Uc = (I x I x I) U, I(i <- a) = cubInterpT[a*cubNq + i]; metric slots of
+ * core/params.h:2-13 (12 per node).  The t-projected slice is cubNq x cubNq
+ * (the reference's s_U is Nq x Nq but indexed up to cubNq x cubNq,
+ * adv.okl:203-231; the two agree for cubNq = Nq).  Parity unpinned, for the
+ * same reason as the dot kernels; checked against exact polynomial answers. */
+void nekbo_adv_cubature(int Nq, int cubNq, int64_t Nelements, const double* vgeo,
+                        const double* cubvgeo, const double* cubD, const double* cubInterpT,
+                        int64_t offset, const double* U, double* NU);
+
 #ifdef __cplusplus
 }
 #endif

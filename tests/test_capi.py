@@ -87,6 +87,19 @@ def test_argument_errors_without_a_launch():
     assert not L.nekb_net_create(8, 16, 4, 1, C.byref(st)) and st.value == nb.ERR_UNSUPPORTED
     assert not L.nekb_net_create(12, 16, 3, 1, C.byref(st)) and st.value == nb.ERR_UNSUPPORTED
     assert not L.nekb_net_load(b"/nonexistent/net.bin", C.byref(st)) and st.value == nb.ERR_INVALID
+    # dot and adv benchmarks
+    assert L.nekb_dot_num_blocks(1000, 256) == 4 and L.nekb_dot_num_blocks(1024, 1024) == 1
+    assert L.nekb_dot_num_blocks(1000, 300) == nb.ERR_INVALID
+    assert L.nekb_dot_partials(3, 10, 1, 0, 256, 1, 1, 1, 1, None) == nb.ERR_INVALID
+    assert L.nekb_dot_partials(1, 10, 1, 0, 512, 1, 1, 1, 1, None) == nb.ERR_INVALID
+    assert L.nekb_dot_partials(2, 10, 2, 5, 256, 1, 1, 1, 1, None) == nb.ERR_INVALID  # offset < N
+    assert L.nekb_dot_partials(0, 10, 1, 0, 256, None, 1, 1, 1, None) == nb.ERR_INVALID
+    assert L.nekb_dot_partials(0, 0, 1, 0, 256, None, None, None, None, None) == nb.OK
+    assert L.nekb_adv_cubature(8, 13, 1, 1, 1, 1, 1, 512, 1, 1, None) == nb.ERR_UNSUPPORTED
+    assert L.nekb_adv_cubature(11, 17, 1, 1, 1, 1, 1, 1331, 1, 1, None) == nb.ERR_UNSUPPORTED
+    assert L.nekb_adv_cubature(8, 12, 2, 1, 1, 1, 1, 512, 1, 1, None) == nb.ERR_INVALID
+    assert L.nekb_adv_cubature(8, 12, 1, None, 1, 1, 1, 512, 1, 1, None) == nb.ERR_INVALID
+    assert L.nekb_adv_cubature(8, 12, 0, None, None, None, None, 0, None, None, None) == nb.OK
 
 
 def test_ogs_host_setup_matches_oracle_without_gpu_kernels():
