@@ -20,6 +20,10 @@
 // reference's summation order (r, then s, then t on the way in; t, s, r on
 // the way out).  Thread (i, j) owns the cubature column (i, j, 0..cubNq-1) for
 // the t-direction passes and the pointwise advection.
+// Where cubNq^2 <= 160 the launch bounds ask for two CTAs per SM (the
+// registers drop from 220 to 168 at cubNq = 12, with a 176-byte spill): the
+// second CTA fills the FP64 pipe while the first waits at a barrier, 11 %
+// faster at N=7, cubN=11 than one CTA per SM.
 //
 // The reference kernel stages the t-projected slice in s_U, declared
 // Nq x Nq, but writes and reads it for all cubNq x cubNq (i, j)
