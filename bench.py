@@ -459,14 +459,28 @@ def dot_adv(nb, torch, dev, E, peak_bw, fp64_peak):
     e1.record()
     torch.cuda.synchronize()
     t = e0.elapsed_time(e1) * 1e-3 / 5
+    NUs = torch.empty_like(U)
+    for _ in range(3):
+        nb.adv_cubature(Nq, cq, Ea, vgeo, cub, D, I, Ea * 512, U, NUs, nb.FP64_SPLIT)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(5):
+        nb.adv_cubature(Nq, cq, Ea, vgeo, cub, D, I, Ea * 512, U, NUs, nb.FP64_SPLIT)
+    e1.record()
+    torch.cuda.synchronize()
+    ts = e0.elapsed_time(e1) * 1e-3 / 5
+    split_diff = float((NUs - NU).abs().max() / NU.abs().max())
     tflops = advmod.flops(Nq, cq) * Ea / t / 1e12
     out["adv"] = {"workload": "advCubatureHex3D_v0, N=7, cubN=11, E=8192, FP64",
                   "ms": t * 1e3, "gdofs": Ea * 343 / t / 1e9, "fp64_tflops": tflops,
                   "fp64_peak_tflops_measured": fp64_peak, "fp64_frac": tflops / fp64_peak,
                   "gbs": advmod.bytes_moved(Nq, cq) * Ea / t / 1e9,
                   "flops_per_element": advmod.flops(Nq, cq),
-                  "bytes_per_element": advmod.bytes_moved(Nq, cq)}
-    del vgeo, cub, U, NU
+                  "bytes_per_element": advmod.bytes_moved(Nq, cq),
+                  "fp64_split": {"ms": ts * 1e3, "gdofs": Ea * 343 / ts / 1e9,
+                                 "speedup_vs_fp64": t / ts,
+                                 "max_rel_diff_to_fp64": split_diff}}
+    del vgeo, cub, U, NU, NUs
     torch.cuda.empty_cache()
     return out
 

@@ -301,10 +301,13 @@ int nekb_dot_partials(int variant, int64_t N, int Nfields, int64_t offset, int b
  * of cubvgeo (12 slots of cubNq^3 per element) and IJW of vgeo (12 slots of
  * Nq^3), slot numbers of core/params.h:2-13.  Built for cubNq = Nq (Nq 2..12)
  * and cubNq = ceil(3 Nq / 2) (Nq 2..10); NEKB_ERR_UNSUPPORTED otherwise.
+ * precision: NEKB_FP64 (native FP64 FMAs; the reference's dfloat = double) or
+ * NEKB_FP64_SPLIT (the same FP64 arrays, arithmetic in double-float on the
+ * FP32 pipes: within ~1e-13 relative of FP64, values in the float range).
  * For cubNq > Nq the reference kernel indexes its Nq x Nq shared tile s_U with
  * cubNq x cubNq indices (adv.okl:203-231); this operator uses a cubNq x cubNq
  * slice there (the two agree for cubNq = Nq).  Asynchronous on the stream. */
-int nekb_adv_cubature(int Nq, int cubNq, int64_t Nelements, const double* vgeo,
+int nekb_adv_cubature(int Nq, int cubNq, int precision, int64_t Nelements, const double* vgeo,
                       const double* cubvgeo, const double* cubD, const double* cubInterpT,
                       int64_t offset, const double* U, double* NU, void* stream);
 

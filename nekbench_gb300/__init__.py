@@ -133,7 +133,7 @@ def lib():
     L.nekb_dot_num_blocks.restype = i64
     L.nekb_dot_num_blocks.argtypes = [i64, i32]
     L.nekb_dot_partials.argtypes = [i32, i64, i32, i64, i32, vp, vp, vp, vp, vp]
-    L.nekb_adv_cubature.argtypes = [i32, i32, i64, vp, vp, vp, vp, i64, vp, vp, vp]
+    L.nekb_adv_cubature.argtypes = [i32, i32, i32, i64, vp, vp, vp, vp, i64, vp, vp, vp]
     if hasattr(L, "nekb_net_create"):
         L.nekb_net_create.restype = vp
         L.nekb_net_create.argtypes = [i32, i32, i32, C.c_uint64, C.POINTER(C.c_int)]
@@ -584,20 +584,24 @@ def load_dot_kernel(name: str, block_size: int = 256, Nfields: int = 1):
     return kernel
 
 
-def adv_cubature(Nq, cubNq, Nelements, vgeo, cubvgeo, cubD, cubInterpT, offset, U, NU, stream=None):
-    """advCubatureHex3D_v0 (adv/kernel/VOLTA/adv.okl:27) on device tensors."""
+def adv_cubature(Nq, cubNq, Nelements, vgeo, cubvgeo, cubD, cubInterpT, offset, U, NU,
+                 precision=FP64, stream=None):
+    """advCubatureHex3D_v0 (adv/kernel/VOLTA/adv.okl:27) on device tensors;
+    precision FP64 or FP64_SPLIT (double-float arithmetic on the FP32 pipes)."""
     _require_cuda(vgeo, cubvgeo, cubD, cubInterpT, U, NU)
-    check(lib().nekb_adv_cubature(Nq, cubNq, Nelements, _ptr(vgeo), _ptr(cubvgeo), _ptr(cubD),
-                                  _ptr(cubInterpT), offset, _ptr(U), _ptr(NU), _stream(stream)))
+    check(lib().nekb_adv_cubature(Nq, cubNq, precision, Nelements, _ptr(vgeo), _ptr(cubvgeo),
+                                  _ptr(cubD), _ptr(cubInterpT), offset, _ptr(U), _ptr(NU),
+                                  _stream(stream)))
 
 
-def load_adv_kernel(N: int, cubN: int):
+def load_adv_kernel(N: int, cubN: int, precision: int = FP64):
     """Kernel object with the adv driver's argument order (adv/main.cpp:115-123):
     ``kernel(Nelements, vgeo, cubvgeo, cubD, cubInterpT, offset, U, NU)``."""
     Nq, cubNq = N + 1, cubN + 1
 
     def kernel(Nelements, vgeo, cubvgeo, cubD, cubInterpT, offset, U, NU):
-        adv_cubature(Nq, cubNq, Nelements, vgeo, cubvgeo, cubD, cubInterpT, offset, U, NU)
+        adv_cubature(Nq, cubNq, Nelements, vgeo, cubvgeo, cubD, cubInterpT, offset, U, NU,
+                     precision)
     kernel.Nq, kernel.cubNq, kernel.name = Nq, cubNq, "advCubatureHex3D_v0"
     return kernel
 

@@ -5,7 +5,12 @@ bandwidth or flop figure; this driver adds the FP64 flops it counts (`flops`)
 and the bytes the operator must move (`bytes`), against which the GPU's FP64
 and HBM roofs are read.
 
-  python -m nekbench_gb300.adv [--N 7] [--cubN 11] [--E 8192] [--steps 10] [--json]
+  python -m nekbench_gb300.adv [--N 7] [--cubN 11] [--E 8192] [--steps 10]
+      [--precision fp64|fp64_split] [--json]
+
+fp64_split evaluates the same operator in double-float arithmetic on the FP32
+pipes and reports its max-norm difference to the FP64 kernel on the same
+inputs.
 
 Inputs as the reference driver builds them (adv/main.cpp:98-112): uniform
 random vgeo, cubvgeo, cubD, cubInterpT and U (here seeded).
@@ -25,6 +30,7 @@ def parse(argv=None):
     p.add_argument("--E", type=int, default=8192)
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--seed", type=int, default=1)
+    p.add_argument("--precision", default="fp64", choices=("fp64", "fp64_split"))
     p.add_argument("--json", action="store_true")
     return p.parse_args(argv)
 
@@ -62,7 +68,8 @@ def main(argv=None):
     cubD, cubI = rand(cq * cq, 22), rand(Nq * cq, 23)
     U = rand(3 * E * Np, 24)
     NU = torch.empty_like(U)
-    kernel = nb.load_adv_kernel(a.N, a.cubN)
+    prec = nb.FP64_SPLIT if a.precision == "fp64_split" else nb.FP64
+    kernel = nb.load_adv_kernel(a.N, a.cubN, prec)
     kernel(E, vgeo, cubvgeo, cubD, cubI, E * Np, U, NU)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -72,10 +79,16 @@ def main(argv=None):
     e1.record()
     torch.cuda.synchronize()
     sec = e0.elapsed_time(e1) * 1e-3 / a.steps
-    res = {"N": a.N, "cubN": a.cubN, "Nelements": E, "NRepetitions": a.steps, "elapsed_s": sec,
+    res = {"N": a.N, "cubN": a.cubN, "Nelements": E, "precision": a.precision,
+           "NRepetitions": a.steps, "elapsed_s": sec,
            "gdofs": E * a.N ** 3 / sec / 1e9, "gflops": flops(Nq, cq) * E / sec / 1e9,
            "gbs": bytes_moved(Nq, cq) * E / sec / 1e9,
            "flops_per_element": flops(Nq, cq), "bytes_per_element": bytes_moved(Nq, cq)}
+    if prec != nb.FP64:
+        ref = torch.empty_like(U)
+        nb.load_adv_kernel(a.N, a.cubN)(E, vgeo, cubvgeo, cubD, cubI, E * Np, U, ref)
+        torch.cuda.synchronize()
+        res["max_rel_diff_to_fp64"] = float((NU - ref).abs().max() / ref.abs().max())
     if a.json:
         print(json.dumps(res))
     else:

@@ -7,13 +7,13 @@
 namespace nekb {
 namespace adv {
 template <int NQ, int CQ>
-int launch(int64_t E, const double* vgeo, const double* cubvgeo, const double* cubD,
+int launch(bool split, int64_t E, const double* vgeo, const double* cubvgeo, const double* cubD,
            const double* cubInterpT, int64_t offset, const double* U, double* NU, cudaStream_t s);
 }  // namespace adv
 
 namespace {
 
-using Launcher = int (*)(int64_t, const double*, const double*, const double*, const double*, int64_t,
+using Launcher = int (*)(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                          const double*, double*, cudaStream_t);
 
 // cubNq = Nq (Nq = 2..12) and the 3/2 rule cubNq = ceil(3 Nq / 2) (Nq = 2..10)
@@ -32,7 +32,8 @@ Launcher find_launcher(int Nq, int cubNq)
 }  // namespace
 }  // namespace nekb
 
-extern "C" int nekb_adv_cubature(int Nq, int cubNq, int64_t Nelements, const double* vgeo,
+extern "C" int nekb_adv_cubature(int Nq, int cubNq, int precision, int64_t Nelements,
+                                 const double* vgeo,
                                  const double* cubvgeo, const double* cubD, const double* cubInterpT,
                                  int64_t offset, const double* U, double* NU, void* stream)
 {
@@ -42,6 +43,8 @@ extern "C" int nekb_adv_cubature(int Nq, int cubNq, int64_t Nelements, const dou
     return fail(NEKB_ERR_UNSUPPORTED,
                 "adv: Nq=%d cubNq=%d not built (cubNq = Nq for Nq 2..12, cubNq = ceil(3 Nq/2) "
                 "for Nq 2..10)", Nq, cubNq);
+  if (precision != NEKB_FP64 && precision != NEKB_FP64_SPLIT)
+    return fail(NEKB_ERR_UNSUPPORTED, "adv: precision %d (NEKB_FP64 or NEKB_FP64_SPLIT)", precision);
   const int64_t Np = (int64_t)Nq * Nq * Nq;
   if (Nelements < 0 || Nelements > INT32_MAX || offset < Nelements * Np)
     return fail(NEKB_ERR_INVALID, "adv: Nelements=%lld offset=%lld (offset >= Nelements*Np)",
@@ -49,6 +52,6 @@ extern "C" int nekb_adv_cubature(int Nq, int cubNq, int64_t Nelements, const dou
   if (Nelements == 0) return NEKB_OK;
   if (!vgeo || !cubvgeo || !cubD || !cubInterpT || !U || !NU)
     return fail(NEKB_ERR_INVALID, "adv: NULL argument");
-  return fn(Nelements, vgeo, cubvgeo, cubD, cubInterpT, offset, U, NU,
+  return fn(precision == NEKB_FP64_SPLIT, Nelements, vgeo, cubvgeo, cubD, cubInterpT, offset, U, NU,
             static_cast<cudaStream_t>(stream));
 }

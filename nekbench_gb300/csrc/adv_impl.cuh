@@ -20,7 +20,8 @@
 // reference's summation order (r, then s, then t on the way in; t, s, r on
 // the way out).  Thread (i, j) owns the cubature column (i, j, 0..cubNq-1) for
 // the t-direction passes and the pointwise advection.
-// Where cubNq^2 <= 160 the launch bounds ask for two CTAs per SM (the
+// Where cubNq^2 <= 160 and two CTAs' shared memory fit on an SM, the FP64
+// kernel's launch bounds ask for two CTAs per SM (the
 // registers drop from 220 to 168 at cubNq = 12, with a 176-byte spill): the
 // second CTA fills the FP64 pipe while the first waits at a barrier, 11 %
 // faster at N=7, cubN=11 than one CTA per SM.
@@ -31,6 +32,7 @@
 // slice is cubNq x cubNq, i.e. the operator the reference's comment names
 // (adv.okl:192).  For cubN = N the two agree.
 #pragma once
+#include "axhelm_x.cuh"
 #include "internal.h"
 
 namespace nekb {
@@ -48,66 +50,119 @@ struct AdvShape {
   static constexpr int nY = 3 * NQ * CQ * CQ;  // [f][c][j][i]: s-interpolated, then t-projected
   static constexpr int nXY = nX + nY > 3 * Cp ? nX + nY : 3 * Cp;  // cubature values [f][k][j][i]
   static constexpr int bytes = 8 * (nI + nD + nU + nXY);
+  // two CTAs per SM: small CTAs whose shared memory fits twice in the SM's 228 KB
+  static constexpr bool two_ctas = threads <= 160 && 2 * (bytes + 1024) <= 228 * 1024;
 };
 
-template <int NQ, int CQ>
-__global__ void __launch_bounds__(CQ * CQ, (CQ * CQ <= 160 ? 2 : 1))
+// Arithmetic of the kernel.  F64: native FP64 FMAs.  DF: every value an
+// unevaluated sum hi + lo of two floats (about 48 significant bits), products
+// and sums with error-free transformations on the FP32 pipes (axhelm_x.cuh);
+// FP64 inputs are split with integer operations and each output rebuilt with
+// one FP64 addition.  Values must lie in the float range (1e-30 .. 1e30).
+struct F64 {
+  using T = double;
+  static constexpr bool kTwoCtas = true;  // where cubNq^2 <= 160
+  struct Acc {
+    double v = 0.0;
+    __device__ __forceinline__ void fma(double a, double b) { v = ::fma(a, b, v); }
+    __device__ __forceinline__ double get() const { return v; }
+  };
+  static __device__ __forceinline__ double in(double d) { return d; }
+  static __device__ __forceinline__ double in_exact(double d) { return d; }
+  static __device__ __forceinline__ double out(double x) { return x; }
+};
+
+struct __align__(8) D2 {
+  float hi, lo;
+};
+
+struct DF {
+  using T = D2;
+  static constexpr bool kTwoCtas = false;  // its temporaries need the registers
+  struct Acc {
+    axx::acc2 a;
+    __device__ __forceinline__ void fma(D2 x, D2 y) { a.fma2(axx::df{x.hi, x.lo}, axx::df{y.hi, y.lo}); }
+    __device__ __forceinline__ D2 get() const
+    {
+      const axx::df r = a.get();
+      return D2{r.hi, r.lo};
+    }
+  };
+  static __device__ __forceinline__ D2 in(double d)
+  {
+    const axx::df r = axx::split(d);
+    return D2{r.hi, r.lo};
+  }
+  // exact two-float split with FP64 arithmetic (operator matrices, once per CTA)
+  static __device__ __forceinline__ D2 in_exact(double d)
+  {
+    const float hi = __double2float_rn(d);
+    return D2{hi, __double2float_rn(d - (double)hi)};
+  }
+  static __device__ __forceinline__ double out(D2 x) { return axx::join(axx::df{x.hi, x.lo}); }
+};
+
+template <int NQ, int CQ, class P>
+__global__ void __launch_bounds__(CQ * CQ, AdvShape<NQ, CQ>::two_ctas && P::kTwoCtas ? 2 : 1)
 k_adv_cubature(const double* __restrict__ vgeo, const double* __restrict__ cubvgeo,
                const double* __restrict__ cubD, const double* __restrict__ cubInterpT,
                int64_t offset, const double* __restrict__ U, double* __restrict__ NU)
 {
   using S = AdvShape<NQ, CQ>;
-  extern __shared__ __align__(16) double sm[];
-  double* sI = sm;           // sI[a CQ + i] = I(i <- a)
-  double* sD = sI + S::nI;   // sD[i CQ + n]
-  double* sU = sD + S::nD;   // [f][c][b][a]
-  double* sX = sU + S::nU;
-  double* sY = sX + S::nX;
-  double* sC = sX;           // [f][k][j][i], over sX and sY
+  using T = typename P::T;
+  using Acc = typename P::Acc;
+  static_assert(sizeof(T) == 8, "shared-memory plan assumes 8-byte values");
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  T* sI = reinterpret_cast<T*>(sm_raw);  // sI[a CQ + i] = I(i <- a)
+  T* sD = sI + S::nI;                    // sD[i CQ + n]
+  T* sU = sD + S::nD;                    // [f][c][b][a]
+  T* sX = sU + S::nU;
+  T* sY = sX + S::nX;
+  T* sC = sX;                            // [f][k][j][i], over sX and sY
 
   const int tid = threadIdx.x, i = tid % CQ, j = tid / CQ;
   const int64_t e = blockIdx.x;
-  for (int n = tid; n < S::nI; n += S::threads) sI[n] = cubInterpT[n];
-  for (int n = tid; n < S::nD; n += S::threads) sD[n] = cubD[n];
+  for (int n = tid; n < S::nI; n += S::threads) sI[n] = P::in_exact(cubInterpT[n]);
+  for (int n = tid; n < S::nD; n += S::threads) sD[n] = P::in_exact(cubD[n]);
   for (int n = tid; n < S::nU; n += S::threads) {
     const int f = n / S::Np;
-    sU[n] = U[f * offset + e * S::Np + (n - f * S::Np)];
+    sU[n] = P::in(U[f * offset + e * S::Np + (n - f * S::Np)]);
   }
   __syncthreads();
 
   // interpolate in r: X[f][c][b][i] = sum_a I(i <- a) U[f][c][b][a]
   for (int n = tid; n < S::nX; n += S::threads) {
     const int ii = n % CQ;
-    const double* u = sU + (n / CQ) * NQ;
-    double acc = 0.0;
+    const T* u = sU + (n / CQ) * NQ;
+    Acc acc;
 #pragma unroll
-    for (int a = 0; a < NQ; ++a) acc = fma(sI[a * CQ + ii], u[a], acc);
-    sX[n] = acc;
+    for (int a = 0; a < NQ; ++a) acc.fma(sI[a * CQ + ii], u[a]);
+    sX[n] = acc.get();
   }
   __syncthreads();
   // interpolate in s: Y[f][c][j][i] = sum_b I(j <- b) X[f][c][b][i]
   for (int n = tid; n < S::nY; n += S::threads) {
     const int ii = n % CQ, jj = (n / CQ) % CQ;
-    const double* x = sX + (n / (CQ * CQ)) * NQ * CQ + ii;
-    double acc = 0.0;
+    const T* x = sX + (n / (CQ * CQ)) * NQ * CQ + ii;
+    Acc acc;
 #pragma unroll
-    for (int b = 0; b < NQ; ++b) acc = fma(sI[b * CQ + jj], x[b * CQ], acc);
-    sY[n] = acc;
+    for (int b = 0; b < NQ; ++b) acc.fma(sI[b * CQ + jj], x[b * CQ]);
+    sY[n] = acc.get();
   }
   __syncthreads();
   // interpolate in t along this thread's column: c[f][k] = sum_c I(k <- c) Y[f][c][j][i]
-  double col[3][CQ];
+  T col[3][CQ];
 #pragma unroll
   for (int f = 0; f < 3; ++f) {
-    double y[NQ];
+    T y[NQ];
 #pragma unroll
     for (int c = 0; c < NQ; ++c) y[c] = sY[((f * NQ + c) * CQ + j) * CQ + i];
 #pragma unroll
     for (int k = 0; k < CQ; ++k) {
-      double acc = 0.0;
+      Acc acc;
 #pragma unroll
-      for (int c = 0; c < NQ; ++c) acc = fma(sI[c * CQ + k], y[c], acc);
-      col[f][k] = acc;
+      for (int c = 0; c < NQ; ++c) acc.fma(sI[c * CQ + k], y[c]);
+      col[f][k] = acc.get();
     }
   }
   __syncthreads();  // X and Y are read: the cubature values take their place
@@ -119,32 +174,46 @@ k_adv_cubature(const double* __restrict__ vgeo, const double* __restrict__ cubvg
 
   // derivatives and the advection term at cubature node (i, j, k)
   const double* g = cubvgeo + e * (int64_t)S::Cp * kNvgeo + j * CQ + i;
-  double adv[3][CQ];
+  T adv[3][CQ];
 #pragma unroll
   for (int k = 0; k < CQ; ++k) {
-    double dr[3], ds[3], dt[3], uc[3];
+    T dr[3], ds[3], dt[3], uc[3];
 #pragma unroll
     for (int f = 0; f < 3; ++f) {
-      const double* c = sC + f * S::Cp;
-      double ar = 0.0, as = 0.0, at = 0.0;
+      const T* c = sC + f * S::Cp;
+      Acc ar, as, at;
 #pragma unroll
       for (int n = 0; n < CQ; ++n) {
-        ar = fma(sD[i * CQ + n], c[(k * CQ + j) * CQ + n], ar);
-        as = fma(sD[j * CQ + n], c[(k * CQ + n) * CQ + i], as);
-        at = fma(sD[k * CQ + n], c[(n * CQ + j) * CQ + i], at);
+        ar.fma(sD[i * CQ + n], c[(k * CQ + j) * CQ + n]);
+        as.fma(sD[j * CQ + n], c[(k * CQ + n) * CQ + i]);
+        at.fma(sD[k * CQ + n], c[(n * CQ + j) * CQ + i]);
       }
-      dr[f] = ar;
-      ds[f] = as;
-      dt[f] = at;
+      dr[f] = ar.get();
+      ds[f] = as.get();
+      dt[f] = at.get();
       uc[f] = c[(k * CQ + j) * CQ + i];
     }
     const double* gk = g + k * CQ * CQ;
-    const double JW = gk[kJW * S::Cp];
-    const double Uhat = JW * (uc[0] * gk[kRX * S::Cp] + uc[1] * gk[kRY * S::Cp] + uc[2] * gk[kRZ * S::Cp]);
-    const double Vhat = JW * (uc[0] * gk[kSX * S::Cp] + uc[1] * gk[kSY * S::Cp] + uc[2] * gk[kSZ * S::Cp]);
-    const double What = JW * (uc[0] * gk[kTX * S::Cp] + uc[1] * gk[kTY * S::Cp] + uc[2] * gk[kTZ * S::Cp]);
+    const T JW = P::in(gk[kJW * S::Cp]);
+    constexpr int slot[3][3] = {{kRX, kRY, kRZ}, {kSX, kSY, kSZ}, {kTX, kTY, kTZ}};
+    T hat[3];  // JW (u . grad r), JW (u . grad s), JW (u . grad t)
 #pragma unroll
-    for (int f = 0; f < 3; ++f) adv[f][k] = Uhat * dr[f] + Vhat * ds[f] + What * dt[f];
+    for (int d = 0; d < 3; ++d) {
+      Acc h;
+#pragma unroll
+      for (int f = 0; f < 3; ++f) h.fma(uc[f], P::in(gk[slot[d][f] * S::Cp]));
+      Acc hj;
+      hj.fma(JW, h.get());
+      hat[d] = hj.get();
+    }
+#pragma unroll
+    for (int f = 0; f < 3; ++f) {
+      Acc a;
+      a.fma(hat[0], dr[f]);
+      a.fma(hat[1], ds[f]);
+      a.fma(hat[2], dt[f]);
+      adv[f][k] = a.get();
+    }
   }
   __syncthreads();  // the cubature values are read: Y takes the t-projection
 
@@ -153,49 +222,60 @@ k_adv_cubature(const double* __restrict__ vgeo, const double* __restrict__ cubvg
   for (int f = 0; f < 3; ++f)
 #pragma unroll
     for (int c = 0; c < NQ; ++c) {
-      double acc = 0.0;
+      Acc acc;
 #pragma unroll
-      for (int k = 0; k < CQ; ++k) acc = fma(sI[c * CQ + k], adv[f][k], acc);
-      sY[((f * NQ + c) * CQ + j) * CQ + i] = acc;
+      for (int k = 0; k < CQ; ++k) acc.fma(sI[c * CQ + k], adv[f][k]);
+      sY[((f * NQ + c) * CQ + j) * CQ + i] = acc.get();
     }
   __syncthreads();
   // project in s: X[f][c][b][i] = sum_j I(j <- b) Y[f][c][j][i]
   for (int n = tid; n < S::nX; n += S::threads) {
     const int ii = n % CQ, b = (n / CQ) % NQ;
-    const double* y = sY + (n / (CQ * NQ)) * CQ * CQ + ii;
-    double acc = 0.0;
+    const T* y = sY + (n / (CQ * NQ)) * CQ * CQ + ii;
+    Acc acc;
 #pragma unroll
-    for (int jj = 0; jj < CQ; ++jj) acc = fma(sI[b * CQ + jj], y[jj * CQ], acc);
-    sX[n] = acc;
+    for (int jj = 0; jj < CQ; ++jj) acc.fma(sI[b * CQ + jj], y[jj * CQ]);
+    sX[n] = acc.get();
   }
   __syncthreads();
   // project in r and apply the inverse mass: NU[f][c][b][a] = IJW sum_i I(i <- a) X[f][c][b][i]
   const double* ijw = vgeo + e * (int64_t)S::Np * kNvgeo + kIJW * S::Np;
   for (int n = tid; n < S::nU; n += S::threads) {
     const int f = n / S::Np, m = n - f * S::Np, a = m % NQ;
-    const double* x = sX + (n / NQ) * CQ;
-    double acc = 0.0;
+    const T* x = sX + (n / NQ) * CQ;
+    Acc acc;
 #pragma unroll
-    for (int ii = 0; ii < CQ; ++ii) acc = fma(sI[a * CQ + ii], x[ii], acc);
-    NU[f * offset + e * S::Np + m] = ijw[m] * acc;
+    for (int ii = 0; ii < CQ; ++ii) acc.fma(sI[a * CQ + ii], x[ii]);
+    Acc scaled;
+    scaled.fma(P::in(ijw[m]), acc.get());
+    NU[f * offset + e * S::Np + m] = P::out(scaled.get());
   }
 }
 
-template <int NQ, int CQ>
-int launch(int64_t E, const double* vgeo, const double* cubvgeo, const double* cubD,
-           const double* cubInterpT, int64_t offset, const double* U, double* NU, cudaStream_t s)
+template <int NQ, int CQ, class P>
+int launch_p(int64_t E, const double* vgeo, const double* cubvgeo, const double* cubD,
+             const double* cubInterpT, int64_t offset, const double* U, double* NU, cudaStream_t s)
 {
   using S = AdvShape<NQ, CQ>;
   static bool configured = false;
   if (!configured) {
-    NEKB_CUDA(cudaFuncSetAttribute(k_adv_cubature<NQ, CQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   S::bytes));
+    NEKB_CUDA(cudaFuncSetAttribute(k_adv_cubature<NQ, CQ, P>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, S::bytes));
     configured = true;
   }
-  k_adv_cubature<NQ, CQ><<<(unsigned)E, S::threads, S::bytes, s>>>(vgeo, cubvgeo, cubD, cubInterpT,
-                                                                   offset, U, NU);
+  k_adv_cubature<NQ, CQ, P><<<(unsigned)E, S::threads, S::bytes, s>>>(vgeo, cubvgeo, cubD,
+                                                                      cubInterpT, offset, U, NU);
   NEKB_CUDA(cudaGetLastError());
   return NEKB_OK;
+}
+
+// split = false: native FP64; true: double-float on the FP32 pipes
+template <int NQ, int CQ>
+int launch(bool split, int64_t E, const double* vgeo, const double* cubvgeo, const double* cubD,
+           const double* cubInterpT, int64_t offset, const double* U, double* NU, cudaStream_t s)
+{
+  return split ? launch_p<NQ, CQ, DF>(E, vgeo, cubvgeo, cubD, cubInterpT, offset, U, NU, s)
+               : launch_p<NQ, CQ, F64>(E, vgeo, cubvgeo, cubD, cubInterpT, offset, U, NU, s);
 }
 
 }  // namespace adv

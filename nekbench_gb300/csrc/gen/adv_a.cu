@@ -3,23 +3,23 @@
 
 namespace nekb {
 namespace adv {
-template int launch<2, 2>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<2, 2>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
-template int launch<3, 3>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<3, 3>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
-template int launch<4, 4>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<4, 4>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
-template int launch<5, 5>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<5, 5>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
-template int launch<6, 6>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<6, 6>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
-template int launch<7, 7>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<7, 7>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
-template int launch<2, 3>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<2, 3>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
-template int launch<3, 5>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<3, 5>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
-template int launch<4, 6>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<4, 6>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
 }  // namespace adv
 }  // namespace nekb

@@ -3,13 +3,13 @@
 
 namespace nekb {
 namespace adv {
-template int launch<8, 8>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<8, 8>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
-template int launch<9, 9>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<9, 9>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
-template int launch<5, 8>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<5, 8>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
-template int launch<6, 9>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<6, 9>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
 }  // namespace adv
 }  // namespace nekb

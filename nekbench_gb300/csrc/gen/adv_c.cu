@@ -3,11 +3,11 @@
 
 namespace nekb {
 namespace adv {
-template int launch<10, 10>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<10, 10>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
-template int launch<7, 11>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<7, 11>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
-template int launch<8, 12>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<8, 12>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
 }  // namespace adv
 }  // namespace nekb

@@ -3,9 +3,9 @@
 
 namespace nekb {
 namespace adv {
-template int launch<11, 11>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<11, 11>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
-template int launch<12, 12>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<12, 12>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
 }  // namespace adv
 }  // namespace nekb

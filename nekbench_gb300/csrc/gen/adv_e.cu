@@ -3,9 +3,9 @@
 
 namespace nekb {
 namespace adv {
-template int launch<9, 14>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<9, 14>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
-template int launch<10, 15>(int64_t, const double*, const double*, const double*, const double*, int64_t,
+template int launch<10, 15>(bool, int64_t, const double*, const double*, const double*, const double*, int64_t,
                             const double*, double*, cudaStream_t);
 }  // namespace adv
 }  // namespace nekb

@@ -95,11 +95,12 @@ def test_argument_errors_without_a_launch():
     assert L.nekb_dot_partials(2, 10, 2, 5, 256, 1, 1, 1, 1, None) == nb.ERR_INVALID  # offset < N
     assert L.nekb_dot_partials(0, 10, 1, 0, 256, None, 1, 1, 1, None) == nb.ERR_INVALID
     assert L.nekb_dot_partials(0, 0, 1, 0, 256, None, None, None, None, None) == nb.OK
-    assert L.nekb_adv_cubature(8, 13, 1, 1, 1, 1, 1, 512, 1, 1, None) == nb.ERR_UNSUPPORTED
-    assert L.nekb_adv_cubature(11, 17, 1, 1, 1, 1, 1, 1331, 1, 1, None) == nb.ERR_UNSUPPORTED
-    assert L.nekb_adv_cubature(8, 12, 2, 1, 1, 1, 1, 512, 1, 1, None) == nb.ERR_INVALID
-    assert L.nekb_adv_cubature(8, 12, 1, None, 1, 1, 1, 512, 1, 1, None) == nb.ERR_INVALID
-    assert L.nekb_adv_cubature(8, 12, 0, None, None, None, None, 0, None, None, None) == nb.OK
+    assert L.nekb_adv_cubature(8, 13, 0, 1, 1, 1, 1, 1, 512, 1, 1, None) == nb.ERR_UNSUPPORTED
+    assert L.nekb_adv_cubature(11, 17, 0, 1, 1, 1, 1, 1, 1331, 1, 1, None) == nb.ERR_UNSUPPORTED
+    assert L.nekb_adv_cubature(8, 12, 0, 2, 1, 1, 1, 1, 512, 1, 1, None) == nb.ERR_INVALID
+    assert L.nekb_adv_cubature(8, 12, 0, 1, None, 1, 1, 1, 512, 1, 1, None) == nb.ERR_INVALID
+    assert L.nekb_adv_cubature(8, 12, nb.FP32, 1, 1, 1, 1, 1, 512, 1, 1, None) == nb.ERR_UNSUPPORTED
+    assert L.nekb_adv_cubature(8, 12, 0, 0, None, None, None, None, 0, None, None, None) == nb.OK
 
 
 def test_ogs_host_setup_matches_oracle_without_gpu_kernels():

@@ -85,8 +85,15 @@ def test_dot_full_size_properties(nb, dev):
     assert abs(a.sum().item() - torch.dot(w * x, y).item()) < 1e-9 * a.sum().item()
 
 
+# tolerance relative to max |NU|: native FP64 (FMA contraction only) and
+# double-float arithmetic (about 48 significant bits)
+ADV_TOL = {0: 1e-12, 4: 1e-12}
+ADV_POLY_TOL = {0: 1e-12, 4: 1e-10}
+
+
+@pytest.mark.parametrize("precision", [0, 4], ids=["fp64", "fp64_split"])
 @pytest.mark.parametrize("Nq,cubNq", ADV_PAIRS)
-def test_adv_matches_oracle(nb, O, dev, Nq, cubNq):
+def test_adv_matches_oracle(nb, O, dev, Nq, cubNq, precision):
     import torch
     E = 5
     case = random_case(Nq, cubNq, E, seed=Nq * 31 + cubNq)
@@ -94,26 +101,30 @@ def test_adv_matches_oracle(nb, O, dev, Nq, cubNq):
     d = {k: _dev(v, dev) for k, v in case.items()}
     NU = torch.full((3 * E * Nq ** 3,), np.nan, dtype=torch.float64, device=dev)
     nb.adv_cubature(Nq, cubNq, E, d["vgeo"], d["cubvgeo"], d["cubD"], d["cubInterpT"], E * Nq ** 3,
-                    d["U"], NU)
+                    d["U"], NU, precision=precision)
     err = np.abs(NU.cpu().numpy() - ref).max()
-    assert err <= 1e-12 * np.abs(ref).max(), err
+    assert err <= ADV_TOL[precision] * np.abs(ref).max(), err
 
 
+@pytest.mark.parametrize("precision", [0, 4], ids=["fp64", "fp64_split"])
 @pytest.mark.parametrize("N,cubN,gauss", [(3, 3, False), (7, 7, False), (7, 11, True), (9, 14, True)])
-def test_adv_exact_polynomials(nb, dev, N, cubN, gauss):
+def test_adv_exact_polynomials(nb, dev, N, cubN, gauss, precision):
     import torch
     E = 4
     inp, exact = polynomial_case(N, cubN, E, gauss)
     d = {k: _dev(v, dev) for k, v in inp.items()}
     NU = torch.empty(3 * E * (N + 1) ** 3, dtype=torch.float64, device=dev)
-    k = nb.load_adv_kernel(N, cubN)
+    k = nb.load_adv_kernel(N, cubN, precision)
     k(E, d["vgeo"], d["cubvgeo"], d["cubD"], d["cubInterpT"], E * (N + 1) ** 3, d["U"], NU)
-    assert np.abs(NU.cpu().numpy() - exact).max() < 1e-12 * max(1.0, np.abs(exact).max())
+    err = np.abs(NU.cpu().numpy() - exact).max()
+    assert err < ADV_POLY_TOL[precision] * max(1.0, np.abs(exact).max()), err
 
 
-def test_adv_full_size_quadratic_and_offset(nb, dev):
+@pytest.mark.parametrize("precision", [0, 4], ids=["fp64", "fp64_split"])
+def test_adv_full_size_quadratic_and_offset(nb, dev, precision):
     """N=7, cubN=11 on 8192 elements (1.36 GB of cubature metric terms): doubling
-    U multiplies NU by exactly 4; a padded field offset gives the same values."""
+    U multiplies NU by exactly 4 (every operation of both arithmetics scales
+    exactly by powers of two); a padded field offset gives the same values."""
     import torch
     Nq, cq, E = 8, 12, 8192
     Np = Nq ** 3
@@ -121,8 +132,8 @@ def test_adv_full_size_quadratic_and_offset(nb, dev):
     r = lambda n: torch.rand(n, dtype=torch.float64, device=dev, generator=g)  # noqa: E731
     vgeo, cub, D, I, U = r(12 * E * Np), r(12 * E * cq ** 3), r(cq * cq), r(Nq * cq), r(3 * E * Np)
     NU1, NU2 = (torch.empty(3 * E * Np, dtype=torch.float64, device=dev) for _ in range(2))
-    nb.adv_cubature(Nq, cq, E, vgeo, cub, D, I, E * Np, U, NU1)
-    nb.adv_cubature(Nq, cq, E, vgeo, cub, D, I, E * Np, 2 * U, NU2)
+    nb.adv_cubature(Nq, cq, E, vgeo, cub, D, I, E * Np, U, NU1, precision)
+    nb.adv_cubature(Nq, cq, E, vgeo, cub, D, I, E * Np, 2 * U, NU2, precision)
     torch.cuda.synchronize()
     assert torch.equal(NU2, 4 * NU1)
     off = E * Np + 64
@@ -130,7 +141,7 @@ def test_adv_full_size_quadratic_and_offset(nb, dev):
     for f in range(3):
         Up[f * off:f * off + E * Np] = U[f * E * Np:(f + 1) * E * Np]
     NUp = torch.zeros(3 * off, dtype=torch.float64, device=dev)
-    nb.adv_cubature(Nq, cq, E, vgeo, cub, D, I, off, Up, NUp)
+    nb.adv_cubature(Nq, cq, E, vgeo, cub, D, I, off, Up, NUp, precision)
     for f in range(3):
         assert torch.equal(NUp[f * off:f * off + E * Np], NU1[f * E * Np:(f + 1) * E * Np])
     assert torch.all(NUp[E * Np:off] == 0)
@@ -144,6 +155,9 @@ def test_adv_errors(nb, dev):
     assert e.value.code == nb.ERR_UNSUPPORTED
     with pytest.raises(nb.NekbError):
         nb.adv_cubature(8, 12, 2, t, t, t, t, 512, t, t)  # offset < E Np
+    with pytest.raises(nb.NekbError) as e:
+        nb.adv_cubature(8, 12, 1, t, t, t, t, 512, t, t, precision=nb.FP32)
+    assert e.value.code == nb.ERR_UNSUPPORTED
     nb.adv_cubature(8, 12, 0, t, t, t, t, 0, t, t)      # no elements: nothing to do
 
 
@@ -156,3 +170,5 @@ def test_drivers(nb, dev):
     assert r["Nblock"] == 500
     r = adv.main(["--E", "256", "--steps", "2", "--json"])
     assert r["gdofs"] > 0 and r["flops_per_element"] == adv.flops(8, 12)
+    r = adv.main(["--E", "256", "--steps", "2", "--precision", "fp64_split", "--json"])
+    assert r["max_rel_diff_to_fp64"] < 1e-12
