@@ -50,8 +50,10 @@ struct AdvShape {
   static constexpr int nY = 3 * NQ * CQ * CQ;  // [f][c][j][i]: s-interpolated, then t-projected
   static constexpr int nXY = nX + nY > 3 * Cp ? nX + nY : 3 * Cp;  // cubature values [f][k][j][i]
   static constexpr int bytes = 8 * (nI + nD + nU + nXY);
+  // with the advection terms [f][k][j][i] staged in shared memory instead of registers
+  static constexpr int bytes_adv = bytes + 8 * 3 * Cp;
   // two CTAs per SM: small CTAs whose shared memory fits twice in the SM's 228 KB
-  static constexpr bool two_ctas = threads <= 160 && 2 * (bytes + 1024) <= 228 * 1024;
+  static constexpr bool fits_twice(int b) { return threads <= 160 && 2 * (b + 1024) <= 228 * 1024; }
 };
 
 // Arithmetic of the kernel.  F64: native FP64 FMAs.  DF: every value an
@@ -61,7 +63,7 @@ struct AdvShape {
 // one FP64 addition.  Values must lie in the float range (1e-30 .. 1e30).
 struct F64 {
   using T = double;
-  static constexpr bool kTwoCtas = true;  // where cubNq^2 <= 160
+  static constexpr __host__ __device__ bool adv_in_smem(int) { return false; }
   struct Acc {
     double v = 0.0;
     __device__ __forceinline__ void fma(double a, double b) { v = ::fma(a, b, v); }
@@ -78,7 +80,12 @@ struct __align__(8) D2 {
 
 struct DF {
   using T = D2;
-  static constexpr bool kTwoCtas = false;  // its temporaries need the registers
+  // On cubature grids of 10^3 nodes and more, the advection terms go to shared
+  // memory: the registers they free let two CTAs share an SM, which the
+  // compensated sums' dependency chains need (N=7, cubN=11: 3.74 ms against
+  // 8.13 ms with the terms in registers).  Smaller grids already run several
+  // CTAs per SM and keep them in registers (N=7, cubN=7: 2.08 against 2.92 ms).
+  static constexpr __host__ __device__ bool adv_in_smem(int cq) { return cq * cq > 96; }
   struct Acc {
     axx::acc2 a;
     __device__ __forceinline__ void fma(D2 x, D2 y) { a.fma2(axx::df{x.hi, x.lo}, axx::df{y.hi, y.lo}); }
@@ -103,7 +110,13 @@ struct DF {
 };
 
 template <int NQ, int CQ, class P>
-__global__ void __launch_bounds__(CQ * CQ, AdvShape<NQ, CQ>::two_ctas && P::kTwoCtas ? 2 : 1)
+constexpr int adv_smem_bytes()
+{
+  return P::adv_in_smem(CQ) ? AdvShape<NQ, CQ>::bytes_adv : AdvShape<NQ, CQ>::bytes;
+}
+
+template <int NQ, int CQ, class P>
+__global__ void __launch_bounds__(CQ * CQ, AdvShape<NQ, CQ>::fits_twice(adv_smem_bytes<NQ, CQ, P>()) ? 2 : 1)
 k_adv_cubature(const double* __restrict__ vgeo, const double* __restrict__ cubvgeo,
                const double* __restrict__ cubD, const double* __restrict__ cubInterpT,
                int64_t offset, const double* __restrict__ U, double* __restrict__ NU)
@@ -111,6 +124,7 @@ k_adv_cubature(const double* __restrict__ vgeo, const double* __restrict__ cubvg
   using S = AdvShape<NQ, CQ>;
   using T = typename P::T;
   using Acc = typename P::Acc;
+  constexpr bool kAdvSmem = P::adv_in_smem(CQ);
   static_assert(sizeof(T) == 8, "shared-memory plan assumes 8-byte values");
   extern __shared__ __align__(16) unsigned char sm_raw[];
   T* sI = reinterpret_cast<T*>(sm_raw);  // sI[a CQ + i] = I(i <- a)
@@ -119,6 +133,7 @@ k_adv_cubature(const double* __restrict__ vgeo, const double* __restrict__ cubvg
   T* sX = sU + S::nU;
   T* sY = sX + S::nX;
   T* sC = sX;                            // [f][k][j][i], over sX and sY
+  T* sA = sX + S::nXY;                   // advection terms [f][k][j][i] (kAdvSmem)
 
   const int tid = threadIdx.x, i = tid % CQ, j = tid / CQ;
   const int64_t e = blockIdx.x;
@@ -174,7 +189,7 @@ k_adv_cubature(const double* __restrict__ vgeo, const double* __restrict__ cubvg
 
   // derivatives and the advection term at cubature node (i, j, k)
   const double* g = cubvgeo + e * (int64_t)S::Cp * kNvgeo + j * CQ + i;
-  T adv[3][CQ];
+  T adv[kAdvSmem ? 1 : 3][kAdvSmem ? 1 : CQ];
 #pragma unroll
   for (int k = 0; k < CQ; ++k) {
     T dr[3], ds[3], dt[3], uc[3];
@@ -212,7 +227,10 @@ k_adv_cubature(const double* __restrict__ vgeo, const double* __restrict__ cubvg
       a.fma(hat[0], dr[f]);
       a.fma(hat[1], ds[f]);
       a.fma(hat[2], dt[f]);
-      adv[f][k] = a.get();
+      if (kAdvSmem)
+        sA[((f * CQ + k) * CQ + j) * CQ + i] = a.get();
+      else
+        adv[kAdvSmem ? 0 : f][kAdvSmem ? 0 : k] = a.get();
     }
   }
   __syncthreads();  // the cubature values are read: Y takes the t-projection
@@ -224,7 +242,9 @@ k_adv_cubature(const double* __restrict__ vgeo, const double* __restrict__ cubvg
     for (int c = 0; c < NQ; ++c) {
       Acc acc;
 #pragma unroll
-      for (int k = 0; k < CQ; ++k) acc.fma(sI[c * CQ + k], adv[f][k]);
+      for (int k = 0; k < CQ; ++k)
+        acc.fma(sI[c * CQ + k], kAdvSmem ? sA[((f * CQ + k) * CQ + j) * CQ + i]
+                                              : adv[kAdvSmem ? 0 : f][kAdvSmem ? 0 : k]);
       sY[((f * NQ + c) * CQ + j) * CQ + i] = acc.get();
     }
   __syncthreads();
@@ -257,14 +277,16 @@ int launch_p(int64_t E, const double* vgeo, const double* cubvgeo, const double*
              const double* cubInterpT, int64_t offset, const double* U, double* NU, cudaStream_t s)
 {
   using S = AdvShape<NQ, CQ>;
+  constexpr int bytes = adv_smem_bytes<NQ, CQ, P>();
+  static_assert(bytes <= 227 * 1024, "adv: shared memory plan exceeds 227 KB");
   static bool configured = false;
   if (!configured) {
     NEKB_CUDA(cudaFuncSetAttribute(k_adv_cubature<NQ, CQ, P>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, S::bytes));
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     configured = true;
   }
-  k_adv_cubature<NQ, CQ, P><<<(unsigned)E, S::threads, S::bytes, s>>>(vgeo, cubvgeo, cubD,
-                                                                      cubInterpT, offset, U, NU);
+  k_adv_cubature<NQ, CQ, P><<<(unsigned)E, S::threads, bytes, s>>>(vgeo, cubvgeo, cubD,
+                                                                   cubInterpT, offset, U, NU);
   NEKB_CUDA(cudaGetLastError());
   return NEKB_OK;
 }
