@@ -1,5 +1,6 @@
 // The dealiased advection operator of nekBench's adv benchmark,
-// advCubatureHex3D_v0 (adv/kernel/VOLTA/adv.okl:27-261), in FP64:
+// advCubatureHex3D_v0 (adv/kernel/VOLTA/adv.okl:27-261), in FP64 (policy F64)
+// or in double-float arithmetic on the FP32 pipes (policy DF):
 //
 //   NU_f = IJW . (I^T x I^T x I^T) [ Uhat dUc_f/dr + Vhat dUc_f/ds + What dUc_f/dt ]
 //   Uc_f = (I x I x I) U_f,   Uhat = JW (Uc . grad r), Vhat = JW (Uc . grad s),
