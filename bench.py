@@ -408,6 +408,48 @@ def nekbone_bp5(nb, torch, dev):
     return out
 
 
+def cpu_pcg_reference(pcg, n_gpu, seconds=2.0, n=16):
+    """The reference's CPU path for the PCG (the oracle's OpenMP restatement:
+    CPU axhelm, gather-scatter and vector kernels as OpenMP loops over all host
+    threads) on a bounded sample of the same problem class as the GPU solves
+    (N=7 perturbed box, lambda0~U[0.5,1.5], lambda1~U[0.5,2.0], Dirichlet,
+    Jacobi): fixed FP64 iterations on E=n^3 elements, about `seconds` of CPU
+    work.  Its time to 1e-8 at the GPU's size is projected: the per-iteration
+    time scaled by the element ratio, times the GPU FP64 solve's iterations."""
+    import oracle as O
+    m = O.BoxMesh(N_ORDER, n, n, n, perturb=0.1, seed=5)
+    L = m.Nlocal
+    lam = np.concatenate([O.uniform(L, 5, 1, 0.5, 1.5), O.uniform(L, 5, 2, 0.5, 2.0)])
+    bp = O.BP(m, lam)
+    f = O.gs_many_add(bp.Ng, bp.offs, bp.gids, O.uniform(L, 5, 3, -1.0, 1.0))
+    f[m.maskIds] = 0.0
+    r, x = f.copy(), np.zeros(L)
+    t0 = time.perf_counter()
+    _, setup = bp.pcg_omp(r, x, 0.0, 5, fixed=True)
+    per = max((time.perf_counter() - t0 - setup) / 5, 1e-6)
+    k = int(min(200, max(10, seconds / per)))
+    r, x = f.copy(), np.zeros(L)
+    t0 = time.perf_counter()
+    it, setup = bp.pcg_omp(r, x, 0.0, k, fixed=True)
+    el = time.perf_counter() - t0 - setup
+    per = el / it
+    out = {"kind": "port", "cores": O.omp_threads(),
+           "sample": f"{it} fixed FP64 Jacobi-PCG iterations on E={n}^3={m.E} elements ({L} local "
+                     f"nodes) of the same problem class, OpenMP over all host threads",
+           "seconds_per_iteration": per,
+           "gdofs_per_iter": m.E * N_ORDER ** 3 / per / 1e9,
+           "setup_s": setup}
+    fp64 = (pcg or {}).get("fp64_jacobi")
+    if fp64:
+        proj = per * (n_gpu ** 3 / m.E) * fp64["iterations"]
+        out["projected_time_to_1e-8_s"] = proj
+        out["projection"] = (f"per-iteration time x (E={n_gpu}^3 / E={n}^3) x the GPU FP64 "
+                             f"solve's {fp64['iterations']} iterations")
+        out["gpu_speedup"] = {k2: proj / v["elapsed_s"] for k2, v in pcg.items()
+                              if isinstance(v, dict) and "elapsed_s" in v}
+    return out
+
+
 def dot_adv(nb, torch, dev, E, peak_bw, fp64_peak):
     """The dot and adv benchmark kernels at N=7.  dot: weightedInnerProduct2_v0
     partials over E elements (3 arrays of E*512 doubles, larger than L2) timed
@@ -607,6 +649,11 @@ def run_gpu(args, rank, ws, local):
     benchmarks = dot_adv(nb, torch, dev, E, peak_bw, fp64_peak)
 
     cpu = CpuAxhelm().rate(args.cpu_seconds) if (rank == 0 and ws == 1) else None
+    if pcg is not None and rank == 0 and ws == 1:
+        try:
+            pcg["cpu_reference_fp64_jacobi"] = cpu_pcg_reference(pcg, args.pcg_n)
+        except Exception as exc:  # a failed baseline must not cost the bench line
+            pcg["cpu_reference_fp64_jacobi"] = {"error": f"{type(exc).__name__}: {exc}"}
     if rank != 0:
         return
     line = {

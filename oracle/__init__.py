@@ -70,6 +70,9 @@ def lib():
     L.nekbo_pcg.argtypes = [C.POINTER(NekboBP), _d, _d, C.c_double, C.c_int, C.c_int, C.c_int,
                             C.c_int, _vp]
     L.nekbo_bp_apply.argtypes = [C.POINTER(NekboBP), _d, _d]
+    L.nekbo_pcg_omp.restype = C.c_int
+    L.nekbo_pcg_omp.argtypes = [C.POINTER(NekboBP), _d, _d, C.c_double, C.c_int, C.c_int, C.c_int,
+                                C.POINTER(C.c_double)]
     L.nekbo_conv3d_forward.argtypes = [C.c_int, C.c_int64, C.c_int, C.c_int, _f, _f, _f]
     L.nekbo_conv3d_backward.argtypes = [C.c_int, C.c_int64, C.c_int, C.c_int, _f, _f, _f, _vp, _f]
     L.nekbo_gelu_forward.argtypes = [C.c_int64, _f, _f]
@@ -229,6 +232,14 @@ class BP:
         it = lib().nekbo_pcg(C.byref(self.s), r, x, tol, maxit, precond, int(flexible), int(fixed),
                              _ptr(h))
         return (it, h) if hist else it
+
+    def pcg_omp(self, r, x, tol, maxit, precond=1, fixed=False):
+        """BPPCG on all host threads (the CPU timing baseline): returns
+        (iterations, set-up seconds)."""
+        setup = C.c_double(0.0)
+        it = lib().nekbo_pcg_omp(C.byref(self.s), r, x, tol, maxit, precond, int(fixed),
+                                 C.byref(setup))
+        return it, setup.value
 
 
 def zero_mean(q, Nloc, Nfields=1, offset=None):

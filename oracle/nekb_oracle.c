@@ -703,6 +703,120 @@ int nekbo_pcg(const nekbo_bp* bp, double* r, double* x, double tol, int maxit, i
   return iter - 1;
 }
 
+/* The same BPPCG on all host threads: the reference's CPU path for this loop
+ * (the OpenMP CPU axhelm of axhelm/kernel/CPU/axhelm.c, the gather-scatter and
+ * the vector kernels of nekBone/kernel/utils.okl run by OCCA's OpenMP
+ * backend).  Every loop over nodes, elements or gather groups is an OpenMP
+ * loop (the groups are disjoint, so they run in parallel without races); the
+ * inner products are OpenMP reductions, so their rounding differs from
+ * nekbo_pcg's ordered sums.  A timing baseline for the CPU, never a parity
+ * reference. */
+static void gs_many_add_omp(int64_t Ngather, const int32_t* offsets, const int32_t* gatherIds, int k,
+                            int64_t stride, double* q)
+{
+  for (int f = 0; f < k; ++f) {
+#pragma omp parallel for schedule(static)
+    for (int64_t g = 0; g < Ngather; ++g) {
+      const int32_t start = offsets[g], end = offsets[g + 1];
+      if (start + 1 == end) continue;
+      double gq = 0;
+      for (int32_t n = start; n < end; ++n) gq += q[gatherIds[n] + f * stride];
+      for (int32_t n = start; n < end; ++n) q[gatherIds[n] + f * stride] = gq;
+    }
+  }
+}
+
+static void bp_apply_omp(const nekbo_bp* bp, const double* q, double* Aq)
+{
+  const int flags = (bp->bk ? NEKBO_AX_BK : 0) | (bp->Nfields == 3 ? NEKBO_AX_N3 : 0);
+  nekbo_axhelm_omp(bp->Nq, bp->Nelements, bp->offset, flags, bp->ggeo, bp->D, bp->lambda, q, Aq);
+  gs_many_add_omp(bp->Ngather, bp->gatherOffsets, bp->gatherIds, bp->Nfields, bp->offset, Aq);
+  for (int f = 0; f < bp->Nfields; ++f) {
+    double* a = Aq + f * bp->offset;
+#pragma omp parallel for schedule(static)
+    for (int64_t n = 0; n < bp->Nmasked; ++n) a[bp->maskIds[n]] = 0.0;
+  }
+}
+
+int nekbo_pcg_omp(const nekbo_bp* bp, double* r, double* x, double tol, int maxit, int precond,
+                  int fixed_iterations, double* setup_s)
+{
+  const double t0 = omp_get_wtime();
+  const int64_t Nloc = bp->Nelements * (int64_t)bp->Nq * bp->Nq * bp->Nq;
+  const int64_t Nall = bp->Nfields * bp->offset;
+  const int NF = bp->Nfields;
+  const int64_t off = bp->offset;
+  double* p = (double*)calloc((size_t)Nall, sizeof(double));
+  double* z = (double*)calloc((size_t)Nall, sizeof(double));
+  double* Ap = (double*)calloc((size_t)Nall, sizeof(double));
+  double* Ax = (double*)calloc((size_t)Nall, sizeof(double));
+  double* invDiag = NULL;
+  const double* w = bp->invDegree;
+  double rdotz1 = 1, rdotz2 = 0, alpha = 0, beta = 0, TOL = 0;
+
+  bp_apply_omp(bp, x, Ax);
+#pragma omp parallel for schedule(static)
+  for (int64_t n = 0; n < Nall; ++n) r[n] = r[n] - Ax[n];
+  if (precond == 1) {
+    int32_t* mapB = (int32_t*)calloc((size_t)Nloc, sizeof(int32_t));
+    for (int64_t m = 0; m < bp->Nmasked; ++m) mapB[bp->maskIds[m]] = 1;
+    invDiag = (double*)calloc((size_t)Nloc, sizeof(double));
+    double* lam = NULL;
+    const double* lamp = bp->lambda;
+    if (bp->bk) {
+      lam = (double*)calloc((size_t)(2 * off), sizeof(double));
+      for (int64_t n = 0; n < off; ++n) lam[n] = 1.0;
+      lamp = lam;
+    }
+    nekbo_update_jacobi(bp->Nq, bp->Nelements, off, mapB, bp->ggeo, bp->D, lamp, invDiag);
+    gs_many_add_omp(bp->Ngather, bp->gatherOffsets, bp->gatherIds, 1, off, invDiag);
+#pragma omp parallel for schedule(static)
+    for (int64_t n = 0; n < Nloc; ++n) invDiag[n] = 1.0 / invDiag[n];
+    free(mapB);
+    free(lam);
+  }
+  if (setup_s) *setup_s = omp_get_wtime() - t0;
+
+  int iter;
+  for (iter = 1; iter <= maxit; ++iter) {
+    double rdotr = 0, rz = 0;
+    for (int f = 0; f < NF; ++f) {
+      double* zf = z + f * off;
+      const double* rf = r + f * off;
+#pragma omp parallel for schedule(static) reduction(+ : rz, rdotr)
+      for (int64_t i = 0; i < Nloc; ++i) {
+        const double zi = precond == 1 ? invDiag[i] * rf[i] : rf[i];
+        zf[i] = zi;
+        rz += rf[i] * zi * w[i];
+        rdotr += rf[i] * rf[i] * w[i];
+      }
+    }
+    rdotz2 = rdotz1;
+    rdotz1 = rz;
+    if (iter == 1) TOL = fmax(tol * tol * rdotr, tol * tol);
+    if (rdotr <= TOL && !fixed_iterations) break;
+    beta = (iter == 1) ? 0 : rdotz1 / rdotz2;
+#pragma omp parallel for schedule(static)
+    for (int64_t n = 0; n < Nall; ++n) p[n] = z[n] + beta * p[n];
+    bp_apply_omp(bp, p, Ap);
+    double pAp = 0;
+    for (int f = 0; f < NF; ++f) {
+      const double* pf = p + f * off;
+      const double* af = Ap + f * off;
+#pragma omp parallel for schedule(static) reduction(+ : pAp)
+      for (int64_t i = 0; i < Nloc; ++i) pAp += pf[i] * af[i] * w[i];
+    }
+    alpha = rdotz1 / pAp;
+#pragma omp parallel for schedule(static)
+    for (int64_t n = 0; n < Nall; ++n) {
+      x[n] = x[n] + alpha * p[n];
+      r[n] = r[n] - alpha * Ap[n];
+    }
+  }
+  free(p); free(z); free(Ap); free(Ax); free(invDiag);
+  return iter - 1;
+}
+
 /* ------------------------------------------------------------------------ */
 /* learned element preconditioner: 3x3x3 convolutions on the Nq^3 nodes of   */
 /* each element with zero padding, tanh-form GELU.                            */

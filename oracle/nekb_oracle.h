@@ -96,6 +96,11 @@ int nekbo_pcg(const nekbo_bp* bp, double* r, double* x, double tol, int maxit, i
  * of every field) / (Nloc*Nfields), over all Nfields*offset entries.  The sum
  * runs in index order (the reference sums 256-wide block partials). */
 void nekbo_zero_mean(int64_t Nloc, int Nfields, int64_t offset, double* q);
+/* BPPCG on all host threads (OpenMP loops and reductions): the CPU timing
+ * baseline of the PCG, not a parity reference.  *setup_s (nullable) receives
+ * the time of the initial residual and the Jacobi set-up. */
+int nekbo_pcg_omp(const nekbo_bp* bp, double* r, double* x, double tol, int maxit, int precond,
+                  int fixed_iterations, double* setup_s);
 /* operator used by the PCG: Aq = mask(gs(axhelm(q))) */
 void nekbo_bp_apply(const nekbo_bp* bp, const double* q, double* Aq);
 double nekbo_wdot(int64_t N, int Nfields, int64_t offset, const double* w, const double* a,

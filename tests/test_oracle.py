@@ -263,3 +263,30 @@ def test_zero_mean_restatement():
     O.zero_mean(q, 30, Nfields=3, offset=40)  # 30 local nodes per field, stride 40
     mean = sum(q0[f * 40:f * 40 + 30].sum() for f in range(3)) / 90
     assert np.allclose(q, q0 - mean, rtol=0, atol=1e-15)
+
+
+def test_openmp_pcg_baseline_matches_serial_oracle():
+    """The CPU timing baseline (BPPCG on all host threads) converges like the
+    ordered oracle PCG: same iteration count within 1, solution within 1e-8."""
+    m = O.BoxMesh(5, 4, 4, 4, perturb=0.1, seed=5)
+    L = m.Nlocal
+    lam = np.concatenate([O.uniform(L, 5, 1, 0.5, 1.5), O.uniform(L, 5, 2, 0.5, 2.0)])
+    bp = O.BP(m, lam)
+    f = O.gs_many_add(bp.Ng, bp.offs, bp.gids, O.uniform(L, 5, 3, -1.0, 1.0))
+    f[m.maskIds] = 0.0
+    r1, x1 = f.copy(), np.zeros(L)
+    it1 = bp.pcg(r1, x1, 1e-10, 1000)
+    r2, x2 = f.copy(), np.zeros(L)
+    it2, setup = bp.pcg_omp(r2, x2, 1e-10, 1000)
+    assert abs(it1 - it2) <= 1 and it1 < 1000 and setup >= 0.0
+    assert np.abs(x1 - x2).max() <= 1e-8 * np.abs(x1).max()
+
+
+def test_bench_cpu_pcg_block_on_a_small_sample():
+    import bench
+    fake = {"fp64_jacobi": {"iterations": 100, "elapsed_s": 2.0}, "mixed_fp32": {"elapsed_s": 0.5}}
+    out = bench.cpu_pcg_reference(fake, 8, seconds=0.05, n=2)
+    assert out["kind"] == "port" and out["cores"] >= 1 and out["seconds_per_iteration"] > 0
+    assert out["projected_time_to_1e-8_s"] == pytest.approx(
+        out["seconds_per_iteration"] * (8 ** 3 / 2 ** 3) * 100)
+    assert set(out["gpu_speedup"]) == {"fp64_jacobi", "mixed_fp32"}
