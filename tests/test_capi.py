@@ -120,3 +120,15 @@ def test_nekbone_summary_formulas_reproduce_the_published_run():
     assert abs(gdofs - 2.09109) < 1e-5
     assert abs(gflops - 393.296) < 1e-3
     assert gbs > 0
+
+
+def test_dot_and_adv_driver_figures():
+    """dot: GDOF/s = Nelements N^3 / t and GB/s = 3 Np 8 Nelements / t
+    (dot/main.cpp:157-159).  adv: the FP64 flops and bytes counted per element
+    at N=7, cubN=11 (interpolation + projection 350,208, derivatives 373,248,
+    pointwise 57,024, inverse mass 1,536; 10 cubature slots + IJW + U + NU)."""
+    from nekbench_gb300 import adv, dot
+    g, b = dot.figures(7, 1000, 2.0)
+    assert g == pytest.approx(1000 * 343 / 2.0 / 1e9) and b == pytest.approx(3 * 512 * 8 * 1000 / 2.0 / 1e9)
+    assert adv.flops(8, 12) == 350208 + 373248 + 57024 + 1536 == 782016
+    assert adv.bytes_moved(8, 12) == 8 * (10 * 1728 + 512 + 6 * 512) == 166912
