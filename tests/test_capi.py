@@ -132,3 +132,17 @@ def test_dot_and_adv_driver_figures():
     assert g == pytest.approx(1000 * 343 / 2.0 / 1e9) and b == pytest.approx(3 * 512 * 8 * 1000 / 2.0 / 1e9)
     assert adv.flops(8, 12) == 350208 + 373248 + 57024 + 1536 == 782016
     assert adv.bytes_moved(8, 12) == 8 * (10 * 1728 + 512 + 6 * 512) == 166912
+
+
+def test_axhelm_driver_figures_reproduce_the_published_runs():
+    """The axhelm driver's figures follow axhelm/main.cpp:161-169: fed the
+    published runs (axhelm/readme.md:31,42; N=7, BK, 4000 elements) they give
+    the printed GDOF/s, GB/s and GFLOP/s."""
+    from nekbench_gb300.axhelm_driver import figures
+    g, b, f = figures(7, 4000, 1, True, 0.00018497)
+    assert g == pytest.approx(7.41742, abs=1e-5)
+    assert b == pytest.approx(797.189, abs=1e-3)
+    assert f == pytest.approx(1229.0, abs=0.5)
+    g, b, f = figures(7, 4000, 1, True, 0.000351181)
+    assert g == pytest.approx(3.90682, abs=1e-5) and b == pytest.approx(419.886, abs=1e-3)
+    assert f == pytest.approx(647.324, abs=1e-3)
