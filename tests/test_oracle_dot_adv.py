@@ -95,3 +95,20 @@ def test_adv_is_quadratic_in_u_and_respects_offset():
     NUo = O.adv_cubature(Nq, cq, E, **dict(case, U=U), offset=off)
     for f in range(3):
         assert np.array_equal(NUo[f * off:f * off + E * Np], NU[f * E * Np:(f + 1) * E * Np])
+
+
+def test_dot_total_matches_the_compiled_reference_inner_product():
+    """Summed in block order, the restated dot partials give the reference's
+    own weighted inner product (nekBone/kernel/CPU/weightedInnerProduct.c:64,
+    compiled unmodified into oracle/_ref) up to summation order: the same
+    quantity, sum over nodes of w x y."""
+    R = O.ref(8)
+    if R is None:
+        pytest.skip("reference CPU kernels not compiled here (oracle/Makefile target ref)")
+    rng = np.random.default_rng(12)
+    N = 300007
+    w, x, y = rng.random((3, N))
+    total = float(np.cumsum(O.dot_partials(0, w, x, y))[-1])
+    wab = np.zeros(2)
+    R.nekref_weighted_inner_product_update(N, N, w, x, y, wab)
+    assert abs(total - wab[0]) <= 1e-13 * abs(wab[0])
