@@ -264,7 +264,9 @@ int nekb_bp_weighted_inner_product2(nekb_bp* bp, const double* w, const double* 
  * library until the process exits; N above 33,554,432 nodes per field is
  * refused with NEKB_ERR_INVALID.  Every call shares that array, so calls that
  * overlap on the same GPU race.  The first call on a device looks up the
- * array's device address; make it before any stream capture. */
+ * array's device address and keeps it for the life of the process; make it
+ * before any stream capture.  A device reset (cudaDeviceReset) is not
+ * supported for this entry point: the kept address would be stale. */
 int nekb_weighted_inner_product_noalloc(int64_t N, int Nfields, int64_t offset, const double* w,
                                         const double* a, const double* b, double* wab,
                                         void* stream);
@@ -343,6 +345,12 @@ int nekb_net_set_weights(nekb_net* net, const float* w);
  * tensor-core inference the arrays must be 16-byte aligned (whole element rows
  * are fetched by bulk copies) and the call returns once the stream is done */
 int nekb_net_forward(nekb_net* net, int64_t E, const float* in, float* out, void* stream);
+/* Sets, from the host, the flag the tensor-core network kernel raises when its
+ * bulk input copies do not arrive within its bounded wait.  The next
+ * nekb_net_forward or learned solve then returns NEKB_ERR_CUDA ("did not
+ * complete in time") and clears the flag.  For tests of that error path: no
+ * device wait has to run out.  No counterpart in the reference. */
+int nekb_net_raise_copy_timeout(void);
 /* one training step on a batch: loss = mean_e |net(in_e) - target_e|^2 / Np;
  * computes gradients with the network's own backward kernels and applies Adam.
  * loss (host) may be NULL. */

@@ -45,7 +45,7 @@ EXPORTED = [
     "nekb_pcg_default_opts", "nekb_bp_pcg", "nekb_bp_zero_mean", "nekb_bp_local_correction",
     "nekb_net_create", "nekb_net_free", "nekb_net_set_inference", "nekb_net_inference",
     "nekb_net_num_params", "nekb_net_get_weights",
-    "nekb_net_set_weights", "nekb_net_forward", "nekb_net_train_step", "nekb_net_gradient",
+    "nekb_net_set_weights", "nekb_net_forward", "nekb_net_raise_copy_timeout", "nekb_net_train_step", "nekb_net_gradient",
     "nekb_net_prepare_pairs", "nekb_net_save", "nekb_net_load", "nekb_peak_fma", "nekb_peak_copy",
     "nekb_dot_num_blocks", "nekb_dot_partials", "nekb_adv_cubature",
 ]
@@ -144,6 +144,7 @@ def lib():
         L.nekb_net_get_weights.argtypes = [vp, vp]
         L.nekb_net_set_weights.argtypes = [vp, vp]
         L.nekb_net_forward.argtypes = [vp, i64, vp, vp, vp]
+        L.nekb_net_raise_copy_timeout.argtypes = []
         L.nekb_net_train_step.argtypes = [vp, i64, vp, vp, C.c_float, vp, vp]
         L.nekb_net_gradient.argtypes = [vp, i64, vp, vp, vp, vp, vp]
         L.nekb_net_prepare_pairs.argtypes = [i32, i64, i64, vp, vp, vp, vp, vp, vp]

@@ -280,12 +280,8 @@ int launch_p(int64_t E, const double* vgeo, const double* cubvgeo, const double*
   using S = AdvShape<NQ, CQ>;
   constexpr int bytes = adv_smem_bytes<NQ, CQ, P>();
   static_assert(bytes <= 227 * 1024, "adv: shared memory plan exceeds 227 KB");
-  static bool configured = false;
-  if (!configured) {
-    NEKB_CUDA(cudaFuncSetAttribute(k_adv_cubature<NQ, CQ, P>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    configured = true;
-  }
+  static SmemOptIn smem_opt;
+  NEKB_TRY(smem_opt.ensure(k_adv_cubature<NQ, CQ, P>, bytes));
   k_adv_cubature<NQ, CQ, P><<<(unsigned)E, S::threads, bytes, s>>>(vgeo, cubvgeo, cubD,
                                                                    cubInterpT, offset, U, NU);
   NEKB_CUDA(cudaGetLastError());

@@ -301,13 +301,9 @@ int run(const AxArgs& a, cudaStream_t s)
 {
   using C = Cfg<NQ, NF, PREC>;
   auto kern = k_axhelm<NQ, NF, BK, PARTIAL, PREC>;
-  // opt in to >48 KB of shared memory once, at the first launch (never inside a
-  // stream capture: the solvers launch every operator once before capturing)
-  static bool smem_attr_set = false;
-  if (C::SMEM > 48 * 1024 && !smem_attr_set) {
-    NEKB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
-    smem_attr_set = true;
-  }
+  // opt in to >48 KB of shared memory at the first launch on each device
+  static SmemOptIn smem_opt;
+  if (C::SMEM > 48 * 1024) NEKB_TRY(smem_opt.ensure(kern, C::SMEM));
   const int64_t nblk = (a.Nelements + C::NEL - 1) / C::NEL;
   if (nblk == 0) return NEKB_OK;
   if (nblk > INT_MAX) return fail(NEKB_ERR_INVALID, "axhelm: too many elements");

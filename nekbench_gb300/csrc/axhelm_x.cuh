@@ -275,11 +275,8 @@ int run(const AxArgs& a, cudaStream_t s)
 {
   using C = CfgX<NQ, NF>;
   auto kern = k_axhelm_x<NQ, NF, BK>;
-  static bool smem_attr_set = false;
-  if (C::SMEM > 48 * 1024 && !smem_attr_set) {
-    NEKB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, C::SMEM));
-    smem_attr_set = true;
-  }
+  static SmemOptIn smem_opt;
+  if (C::SMEM > 48 * 1024) NEKB_TRY(smem_opt.ensure(kern, C::SMEM));
   const int64_t nblk = (a.Nelements + C::NEL - 1) / C::NEL;
   if (nblk == 0) return NEKB_OK;
   if (nblk > INT_MAX) return fail(NEKB_ERR_INVALID, "axhelm: too many elements");

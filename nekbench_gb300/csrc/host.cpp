@@ -134,13 +134,18 @@ void deriv_matrix(int Nq, const double* r, double* D)
 // ------------------------------------------------------------------ gather-scatter setup
 // Restates the local branch of ogsSetup (3rdParty/ogs/src/ogsSetup.cpp:137-212)
 // and the degree vector (:325-352) with linear-time passes:
-//  1. nodes with id != 0 are grouped by |id| with a stable counting sort (a
-//     stable comparison sort when ids are sparse), so members stay in
-//     ascending local index inside a group;
-//  2. groups are numbered by the local index of their first member, which is
+//  1. nodes with id != 0 are ordered by |id| with a stable counting sort (a
+//     stable comparison sort when ids are sparse), so nodes of equal |id|
+//     stay in ascending local index: the (|id|, localId) order of the
+//     reference's qsort (:40-54, 156);
+//  2. a group is a run of equal SIGNED id in that order: the reference opens
+//     a new gather node whenever the signed id differs from its predecessor
+//     (:161-166), so ids 5,-5,5 at local indices 0,1,2 make three groups;
+//  3. groups are numbered by the local index of their first member, which is
 //     the order the reference's re-sort by local id produces (:173-189);
-//  3. CSR offsets/ids in that order; invDegree = 1/size (1 for id-0 nodes).
-// The result is bit-identical to the reference CSR for any id array.
+//  4. CSR offsets/ids in that order; invDegree = 1/size (1 for id-0 nodes).
+// The result is bit-identical to the reference CSR for any id array, signed
+// ids included.
 int nekb_ogs_build(nekb_ogs* o, int64_t N, const int64_t* ids)
 {
   using namespace nekb;
@@ -172,11 +177,11 @@ int nekb_ogs_build(nekb_ogs* o, int64_t N, const int64_t* ids)
     std::stable_sort(order.begin(), order.end(),
                      [&](int32_t a, int32_t b) { return key[a] < key[b]; });
   }
-  // runs of equal key: run r spans order[rs[r] .. rs[r+1])
+  // runs of equal signed id: run r spans order[rs[r] .. rs[r+1])
   std::vector<int64_t> rs;
   rs.reserve(Nl / 2 + 2);
   for (int64_t p = 0; p < Nl; ++p)
-    if (p == 0 || key[order[p]] != key[order[p - 1]]) rs.push_back(p);
+    if (p == 0 || ids[lid[order[p]]] != ids[lid[order[p - 1]]]) rs.push_back(p);
   rs.push_back(Nl);
   const int64_t Ng = (int64_t)rs.size() - 1;
   o->NlocalGather = Ng;

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
+#include <atomic>
 #include <cstdint>
 #include <vector>
 
@@ -27,6 +28,26 @@ void clear_error();
     int nekb_s_ = (call);               \
     if (nekb_s_ != NEKB_OK) return nekb_s_; \
   } while (0)
+
+// Opt-in of one kernel to more than 48 KB of dynamic shared memory.  The
+// attribute belongs to each device's context, so it is set once per device
+// (ordinals 0..63 are remembered; beyond that it is set at every launch).  The
+// solvers launch every operator once before they capture a graph, so the
+// first launch on a device never falls inside a capture.
+struct SmemOptIn {
+  std::atomic<uint64_t> done{0};
+  template <typename K>
+  int ensure(K kern, int bytes)
+  {
+    int dev = 0;
+    NEKB_CUDA(cudaGetDevice(&dev));
+    const uint64_t bit = (dev >= 0 && dev < 64) ? (uint64_t(1) << dev) : 0;
+    if (bit != 0 && (done.load(std::memory_order_acquire) & bit) != 0) return 0;
+    NEKB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    done.fetch_or(bit, std::memory_order_release);
+    return 0;
+  }
+};
 
 constexpr int kMaxNq = 14;      // FP64; the other precisions go to kMaxNqReduced
 constexpr int kMaxNqReduced = 12;

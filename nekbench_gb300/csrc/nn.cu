@@ -542,11 +542,8 @@ int run_infer(const nekb_net* net, int64_t Etot, int64_t Efield, const float* r,
               const float* invDiag, float* out, int normalize, const int* skip, cudaStream_t s)
 {
   constexpr int SM = infer_smem<NQ, C>();
-  static bool attr = false;
-  if (!attr) {
-    NEKB_CUDA(cudaFuncSetAttribute(k_net_infer<NQ, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
-    attr = true;
-  }
+  static SmemOptIn smem_opt;
+  NEKB_TRY(smem_opt.ensure(k_net_infer<NQ, C>, SM));
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -565,11 +562,8 @@ template <int NQ, int C>
 int run_train(nekb_net* net, int64_t E, const float* in, const float* target, cudaStream_t s)
 {
   constexpr int SM = train_smem<NQ, C>();
-  static bool attr = false;
-  if (!attr) {
-    NEKB_CUDA(cudaFuncSetAttribute(k_net_train<NQ, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, SM));
-    attr = true;
-  }
+  static SmemOptIn smem_opt;
+  NEKB_TRY(smem_opt.ensure(k_net_train<NQ, C>, SM));
   int64_t grid = net->gblocks;
   if (grid > E) grid = E;
   const float gscale = 2.0f / (float)(E * np_of(NQ));
@@ -745,6 +739,8 @@ int nekb_net_set_weights(nekb_net* net, const float* w)
   if (!net || !w) return fail(NEKB_ERR_INVALID, "net: NULL");
   return net_upload(net, w);
 }
+
+int nekb_net_raise_copy_timeout(void) { return net_tc_raise_copy_timeout(); }
 
 int nekb_net_forward(nekb_net* net, int64_t E, const float* in, float* out, void* stream)
 {

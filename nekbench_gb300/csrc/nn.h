@@ -25,5 +25,8 @@ int net_infer_tc(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const f
 // NEKB_OK, or an error (and the flag cleared) when a tensor-core launch gave up
 // waiting for its input copies since the last call
 int net_tc_copy_timeout();
+// sets the timeout flag from the host, as the kernel does when an input copy
+// does not complete (for tests of the error path; no device wait runs out)
+int net_tc_raise_copy_timeout();
 
 }  // namespace nekb

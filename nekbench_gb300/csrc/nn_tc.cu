@@ -408,6 +408,13 @@ int net_tc_copy_timeout()
   return NEKB_OK;
 }
 
+int net_tc_raise_copy_timeout()
+{
+  const int one = 1;
+  NEKB_CUDA(cudaMemcpyToSymbol(g_tc_copy_timeout, &one, sizeof(int)));
+  return NEKB_OK;
+}
+
 bool net_tc_supported(int Nq, int C) { return Nq == kNq && C == 16; }
 
 int net_infer_tc(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const float* r,
@@ -418,11 +425,8 @@ int net_infer_tc(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const f
   for (const void* p : {(const void*)r, (const void*)w, (const void*)invDiag})
     if (reinterpret_cast<uintptr_t>(p) % 16 != 0)
       return fail(NEKB_ERR_INVALID, "network: input arrays must be 16-byte aligned");
-  static bool attr = false;
-  if (!attr) {
-    NEKB_CUDA(cudaFuncSetAttribute(k_net_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmTotal));
-    attr = true;
-  }
+  static SmemOptIn smem_opt;
+  NEKB_TRY(smem_opt.ensure(k_net_infer_tc, kSmTotal));
   int dev = 0, sms = 152, per_sm = 0;
   NEKB_CUDA(cudaGetDevice(&dev));
   NEKB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

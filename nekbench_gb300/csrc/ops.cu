@@ -76,7 +76,13 @@ inline unsigned grid_for(int64_t n, int threads, int64_t cap = 152 * 16)
 }
 
 // ------------------------------------------------------------------ Jacobi diagonal
-// updateJacobi (nekBone/kernel/updateJacobi.okl:27-108): one thread per node.
+// updateJacobi (nekBone/kernel/updateJacobi.okl:27-108): one thread per node,
+// the reference's terms in its order.  Every product and sum is an explicitly
+// rounded FP64 operation (no fused multiply-add), so the diagonal is bit for
+// bit the CPU statement's; the kernel runs once per solve.
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+
 template <bool bk>
 __global__ void k_update_jacobi(int Nq, int64_t E, int64_t offset, const int32_t* __restrict__ mapB,
                                 const double* __restrict__ ggeo, const double* __restrict__ D,
@@ -96,18 +102,22 @@ __global__ void k_update_jacobi(int Nq, int64_t E, int64_t offset, const int32_t
       const double lam0 = bk ? 1.0 : l0[n];
       const double lam1 = bk ? 0.0 : lambda[id + offset];
       const double Dii = D[i * Nq + i], Djj = D[j * Nq + j], Dkk = D[k * Nq + k];
+      // 2 * G * lambda0 * Da * Db, left to right
+      auto cross = [&](int slot, double Da, double Db) {
+        return mul_rn(mul_rn(mul_rn(mul_rn(2.0, g[slot * Np + n]), lam0), Da), Db);
+      };
       r_q = 0.0;
-      r_q += 2.0 * g[2 * Np + n] * lam0 * Dii * Djj;
-      r_q += 2.0 * g[3 * Np + n] * lam0 * Dii * Dkk;
-      r_q += 2.0 * g[5 * Np + n] * lam0 * Djj * Dkk;
+      r_q = add_rn(r_q, cross(2, Dii, Djj));
+      r_q = add_rn(r_q, cross(3, Dii, Dkk));
+      r_q = add_rn(r_q, cross(5, Djj, Dkk));
       for (int m = 0; m < Nq; ++m) {
         const int nr = m + Nq * (j + Nq * k), ns = i + Nq * (m + Nq * k), nt = i + Nq * (j + Nq * m);
         const double dmi = D[m * Nq + i], dmj = D[m * Nq + j], dmk = D[m * Nq + k];
-        r_q += g[1 * Np + nr] * (bk ? 1.0 : l0[nr]) * dmi * dmi;
-        r_q += g[4 * Np + ns] * (bk ? 1.0 : l0[ns]) * dmj * dmj;
-        r_q += g[6 * Np + nt] * (bk ? 1.0 : l0[nt]) * dmk * dmk;
+        r_q = add_rn(r_q, mul_rn(mul_rn(mul_rn(g[1 * Np + nr], bk ? 1.0 : l0[nr]), dmi), dmi));
+        r_q = add_rn(r_q, mul_rn(mul_rn(mul_rn(g[4 * Np + ns], bk ? 1.0 : l0[ns]), dmj), dmj));
+        r_q = add_rn(r_q, mul_rn(mul_rn(mul_rn(g[6 * Np + nt], bk ? 1.0 : l0[nt]), dmk), dmk));
       }
-      r_q += g[n] * lam1;
+      r_q = add_rn(r_q, mul_rn(g[n], lam1));
     }
     diag[id] = r_q;
   }

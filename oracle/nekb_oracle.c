@@ -430,8 +430,10 @@ int nekbo_omp_threads(void)
 /* ------------------------------------------------------------------------ */
 /* ogs: local branch of ogsSetup (3rdParty/ogs/src/ogsSetup.cpp:137-212) and  */
 /* invDegree (:325-352).  Nodes with id 0 are skipped (:127,145).  Nodes are  */
-/* sorted by (|id|, localId) (:40-52,156); gather nodes are then numbered in  */
-/* order of their first (lowest) local index (:173-189); each group lists its */
+/* sorted by (|id|, localId) (:40-52,156) and a new gather node starts at     */
+/* every change of the signed id in that order (:161-166), so a run such as   */
+/* 5, -5, 5 makes three gather nodes; gather nodes are then numbered in order */
+/* of their first (lowest) local index (:173-189); each group lists its       */
 /* members in ascending local index (:197-205).                               */
 /* ------------------------------------------------------------------------ */
 typedef struct {
@@ -489,9 +491,9 @@ int64_t nekbo_ogs_setup(int64_t N, const int64_t* ids, int32_t* offsets, int32_t
   nodes[0].owned = 1;
   for (int64_t i = 1; i < Nlocal; ++i) {
     int s = 0;
-    int64_t a = nodes[i].baseId < 0 ? -nodes[i].baseId : nodes[i].baseId;
-    int64_t b = nodes[i - 1].baseId < 0 ? -nodes[i - 1].baseId : nodes[i - 1].baseId;
-    if (a != b) { Ngather++; s = 1; }
+    /* the sort keys on |id|, but a group ends wherever the SIGNED id changes
+     * (ogsSetup.cpp:161-166): ids 5 and -5 never share a group */
+    if (nodes[i].baseId != nodes[i - 1].baseId) { Ngather++; s = 1; }
     nodes[i].newId = Ngather;
     nodes[i].owned = s;
   }

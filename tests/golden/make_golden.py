@@ -38,6 +38,27 @@ def axhelm_case(N, nx, ny, nz, seed):
     return out
 
 
+def config1_case(seed=1, stride=61):
+    """axhelm FP64 Poisson at N=7 on the perturbed 8x8x8 box (E=512, 262,144
+    local nodes): axhelmReference.cpp with lambda=0 (the BK operator).  The
+    full output is 2 MB, so the fixture keeps every stride-th node and the
+    whole array's sum, sum of squares and max-abs; the inputs are rebuilt from
+    the seed by the oracle's box mesh and generator."""
+    N, n = 7, 8
+    Nq = N + 1
+    R = O.ref(Nq)
+    assert R is not None, f"oracle/_ref/libnekref_nq{Nq}.so missing: run make -C oracle ref"
+    m = O.BoxMesh(N, n, n, n, perturb=0.1, seed=seed)
+    E, L = m.E, m.Nlocal
+    q = O.uniform(L, seed, 3, -1.0, 1.0)
+    Aq = np.zeros(L)
+    R.nekref_axhelm_reference(Nq, E, 0.0, m.ggeo, m.D, q.copy(), Aq)
+    idx = np.arange(0, L, stride, dtype=np.int64)
+    return {"N": N, "n": n, "seed": seed, "idx": idx, "Aq_samples": Aq[idx],
+            "ggeo_samples": m.ggeo[idx], "q_samples": q[idx],
+            "Aq_sum": Aq.sum(), "Aq_sumsq": (Aq * Aq).sum(), "Aq_maxabs": np.abs(Aq).max()}
+
+
 def wip_case(Nq, n, seed):
     R = O.ref(Nq)
     w = O.uniform(n, seed, 1, 0.1, 1.0)
@@ -53,6 +74,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "axhelm_n7.npz"), **axhelm_case(7, 2, 1, 1, 12))
     np.savez_compressed(os.path.join(HERE, "axhelm_n9.npz"), **axhelm_case(9, 1, 1, 1, 13))
     np.savez_compressed(os.path.join(HERE, "weighted_inner_product.npz"), **wip_case(8, 1000, 14))
+    np.savez_compressed(os.path.join(HERE, "axhelm_config1_e512.npz"), **config1_case())
     rng = {"u_seed5_stream2": O.uniform(16, 5, 2), "u_seed0_stream0": O.uniform(16, 0, 0)}
     np.savez_compressed(os.path.join(HERE, "uniform.npz"), **rng)
     print("golden vectors written to", HERE)

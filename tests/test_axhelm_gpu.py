@@ -252,3 +252,35 @@ def test_axhelm_driver(N, ndim, bk):
     assert rs["max_rel_diff_to_fp64"] < 1e-12
     r32 = drv.main(base + ["--precision", "fp32"])
     assert r32["max_rel_diff_to_fp64"] < 1e-5
+
+
+def test_config1_e512_against_axhelm_reference(nb, O, dev):
+    """The first configuration at its stated size: FP64 Poisson (BK), N=7,
+    E=8x8x8=512 elements of the perturbed unit box (262,144 local nodes),
+    q ~ U[-1,1].  Compared with axhelmReference.cpp's output (the fixture
+    tests/golden/axhelm_config1_e512.npz: 4298 sampled nodes plus the whole
+    array's sum, sum of squares and max-abs) and, at every node, with the
+    oracle; 1e-12 relative (max-norm), the FP64 bar."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                             "axhelm_config1_e512.npz"))
+    N, n, seed = int(g["N"]), int(g["n"]), int(g["seed"])
+    m = O.BoxMesh(N, n, n, n, perturb=0.1, seed=seed)
+    E, L = m.E, m.Nlocal
+    assert E == 512 and L == 262144
+    q = O.uniform(L, seed, 3, -1.0, 1.0)
+    idx = g["idx"]
+    assert rel(m.ggeo[idx], g["ggeo_samples"]) < 1e-14 and np.array_equal(q[idx], g["q_samples"])
+    for name in ("axhelm_bk_v0",):
+        k = nb.load_ax_kernel(name, N)
+        Aq = torch.zeros(L, dtype=torch.float64, device=dev)
+        k(E, L, T(m.ggeo, dev), T(m.D, dev), torch.zeros(2 * L, dtype=torch.float64, device=dev),
+          T(q, dev), Aq)
+        torch.cuda.synchronize()
+        got = Aq.cpu().numpy()
+        scale = float(g["Aq_maxabs"])
+        assert np.abs(got[idx] - g["Aq_samples"]).max() / scale < 1e-12
+        assert abs(np.abs(got).max() - scale) / scale < 1e-12
+        assert abs((got * got).sum() - float(g["Aq_sumsq"])) / float(g["Aq_sumsq"]) < 1e-12
+        ref = O.axhelm(N + 1, E, L, nb.AX_BK, m.ggeo, m.D, np.zeros(2 * L), q)
+        assert rel(got, ref) < 1e-12

@@ -204,3 +204,34 @@ def test_fcg_window_with_a_zero_network_matches_jacobi(nb, O, dev):
     with pytest.raises(nb.NekbError):
         bp.pcg(lam, f.clone(), torch.zeros_like(f), 1e-8, 10, solver=nb.SOLVER_MIXED,
                precond=nb.PRECOND_LEARNED, net=net, fcg_window=9)
+
+
+def test_copy_timeout_flag_becomes_an_error_status(nb, O, dev):
+    """The tensor-core kernel's bounded wait on its bulk input copies ends, if
+    the copies never arrive, by raising a device flag; the host turns the flag
+    into NEKB_ERR_CUDA.  Here the flag is raised from the host (no device wait
+    runs out): the next forward and the next learned solve report the error,
+    each clears the flag, and the call after it succeeds."""
+    net = nb.Net(8, 16, 3, seed=5)
+    assert net.inference == nb.NET_TENSOR
+    E = 4
+    x = torch.from_numpy(O.uniform(E * 512, 15, 1, -1, 1).astype(np.float32)).to(dev)
+    out = torch.zeros(E * 512, dtype=torch.float32, device=dev)
+    net.forward(x, out, E)
+    nb.check(nb.lib().nekb_net_raise_copy_timeout())
+    with pytest.raises(nb.NekbError, match="did not complete in time") as ei:
+        net.forward(x, out, E)
+    assert ei.value.code == nb.ERR_CUDA
+    net.forward(x, out, E)  # the flag was cleared with the report
+    bp = nb.BP(7, 3, 3, 3, perturb=0.1, seed=3)
+    L = bp.Nlocal
+    lam = torch.cat([torch.full((L,), 1.0), torch.full((L,), 1.5)]).double().to(dev)
+    f = torch.from_numpy(O.uniform(L, 8, 3, -1, 1)).to(dev)
+    bp.ogs.gather_scatter_many(f)
+    nb.check(nb.lib().nekb_net_raise_copy_timeout())
+    with pytest.raises(nb.NekbError, match="did not complete in time"):
+        bp.pcg(lam, f.clone(), torch.zeros_like(f), 1e-8, 2000, solver=nb.SOLVER_MIXED,
+               precond=nb.PRECOND_LEARNED, net=net)
+    st = bp.pcg(lam, f.clone(), torch.zeros_like(f), 1e-8, 2000, solver=nb.SOLVER_MIXED,
+                precond=nb.PRECOND_LEARNED, net=net)
+    assert st["status"] == 0 and st["true_rel_res"] <= 1e-8

@@ -35,6 +35,32 @@ def test_axhelm_matches_reference_golden(case):
         assert rel(got, g[f"Aq_reference_lam{lam1}"]) < 1e-14
 
 
+def config1_inputs(g):
+    """Rebuild the E=512 (8x8x8, N=7) perturbed box and q of the config-1
+    fixture from its seed; the fixture's samples confirm the rebuild."""
+    N, n, seed = int(g["N"]), int(g["n"]), int(g["seed"])
+    m = O.BoxMesh(N, n, n, n, perturb=0.1, seed=seed)
+    q = O.uniform(m.Nlocal, seed, 3, -1.0, 1.0)
+    idx = g["idx"]
+    assert rel(m.ggeo[idx], g["ggeo_samples"]) < 1e-14
+    assert np.array_equal(q[idx], g["q_samples"])
+    return m, q
+
+
+def test_axhelm_config1_size_against_reference():
+    """axhelm FP64 Poisson, N=7, E=8^3=512 perturbed box: the oracle's BK
+    operator against axhelmReference.cpp's output (lambda = 0) at 4298
+    sampled nodes and the whole array's sum, sum of squares and max-abs."""
+    g = np.load(os.path.join(GOLD, "axhelm_config1_e512.npz"))
+    m, q = config1_inputs(g)
+    got = O.axhelm(m.Nq, m.E, m.Nlocal, O.AX_BK, m.ggeo, m.D, np.zeros(2 * m.Nlocal), q)
+    scale = float(g["Aq_maxabs"])
+    assert np.abs(got[g["idx"]] - g["Aq_samples"]).max() / scale < 1e-13
+    assert abs(np.abs(got).max() - scale) / scale < 1e-13
+    assert abs((got * got).sum() - float(g["Aq_sumsq"])) / float(g["Aq_sumsq"]) < 1e-12
+    assert abs(got.sum() - float(g["Aq_sum"])) / (scale * m.Nlocal) < 1e-13
+
+
 def test_uniform_generator_golden():
     g = np.load(os.path.join(GOLD, "uniform.npz"))
     assert np.array_equal(O.uniform(16, 5, 2), g["u_seed5_stream2"])
@@ -149,6 +175,53 @@ def test_ogs_csr_order():
         assert np.all(np.diff(mem) > 0) and len(set(ids[mem])) == 1
         assert np.all(invdeg[mem] == 1.0 / len(mem))
     assert np.all(invdeg[ids == 0] == 1.0)
+
+
+def ogs_setup_statement(ids):
+    """Plain-Python statement of ogsSetup's local branch
+    (3rdParty/ogs/src/ogsSetup.cpp:40-54, 137-212): order the nonzero ids by
+    (|id|, local index), open a gather node at every change of the SIGNED id
+    (:161-166), number the gather nodes by the local index of their first
+    member (:173-189), list members in ascending local index (:197-205)."""
+    nodes = sorted((abs(int(v)), i, int(v)) for i, v in enumerate(ids) if v != 0)
+    groups = []
+    for p, (_, lid, sid) in enumerate(nodes):
+        if p == 0 or sid != nodes[p - 1][2]:
+            groups.append([])
+        groups[-1].append(lid)
+    groups.sort(key=lambda g: g[0])
+    offs = np.cumsum([0] + [len(g) for g in groups]).astype(np.int32)
+    gids = np.array([n for g in groups for n in g], dtype=np.int32)
+    invdeg = np.ones(len(ids))
+    for g in groups:
+        invdeg[g] = 1.0 / len(g)
+    return len(groups), offs, gids, invdeg
+
+
+@pytest.mark.parametrize("ids", [[5, -5, 5], [5, 5, -5], [-5, 5, 5], [-3, -3, 3, 0, 3, -3],
+                                 [7, -7], [-7, -7], [0, 0, 0]])
+def test_ogs_signed_ids_small(ids):
+    ids = np.array(ids, dtype=np.int64)
+    got = O.ogs_setup(ids)
+    ref = ogs_setup_statement(ids)
+    assert got[0] == ref[0]
+    for a, b in zip(got[1:], ref[1:]):
+        assert np.array_equal(a, b)
+    if list(ids) == [5, -5, 5]:
+        assert got[0] == 3  # one gather node per change of sign, as ogsSetup.cpp:163
+
+
+def test_ogs_signed_ids_random():
+    rng = np.random.default_rng(11)
+    for n, hi in ((50, 5), (2000, 60), (3000, 10**12)):
+        ids = rng.integers(0, hi, size=n).astype(np.int64)
+        ids[rng.random(n) < 0.4] *= -1
+        ids[rng.random(n) < 0.1] = 0
+        got = O.ogs_setup(ids)
+        ref = ogs_setup_statement(ids)
+        assert got[0] == ref[0]
+        for a, b in zip(got[1:], ref[1:]):
+            assert np.array_equal(a, b)
 
 
 def _problem(N=3, n=3, seed=4):
