@@ -141,9 +141,12 @@ class ClockSampler:
 
 # ------------------------------------------------------------------ CPU baseline
 class CpuAxhelm:
-    """The reference's CPU axhelm (the oracle's restatement, bit-identical to
-    axhelm/kernel/CPU/axhelm.c; OpenMP over elements, all host threads) on a
-    bounded sample of the workload: n_el elements of the same N=7 perturbed box."""
+    """The reference's CPU axhelm (axhelm/kernel/CPU/axhelm.c restated in
+    oracle/cpu_axhelm.c with the order fixed at compile time and the
+    reference's -O3, as the reference builds it; OpenMP over elements, all host
+    threads; within a few per cent of the compiled reference on the same cores)
+    on a bounded sample of the workload: n_el elements of the same N=7
+    perturbed box."""
 
     def __init__(self, n_el=4096):
         import oracle as O
@@ -154,8 +157,7 @@ class CpuAxhelm:
 
     def apply(self):
         m = self.m
-        self.O.axhelm_omp(N_ORDER + 1, m.E, m.Nlocal, self.O.AX_BK, m.ggeo, m.D, None, self.q,
-                          self.Aq)
+        self.O.cpu_axhelm(N_ORDER + 1, True, m.E, m.Nlocal, m.ggeo, m.D, None, self.q, self.Aq)
 
     def rate(self, seconds):
         self.apply()  # warm-up
@@ -171,7 +173,7 @@ class CpuAxhelm:
                 "cores": self.O.omp_threads(), "kind": "port",
                 "sample": f"{reps} applications of FP64 BK axhelm on {self.m.E} elements (N=7, "
                           f"{self.m.Nlocal} nodes) of the same perturbed box in {el:.1f} s, "
-                          f"OpenMP over elements"}
+                          f"compile-time order, -O3, OpenMP over elements"}
 
 
 def run_reference(args, rank, ws):
@@ -295,8 +297,9 @@ def measured_bf16():
     return 1900.0
 
 
-def pcg_comparison(nb, torch, dev, n, learned):
-    """Three solvers on the same problem to true FP64 relative residual 1e-8."""
+def pcg_comparison(nb, torch, dev, n, learned, names=None):
+    """Three solvers on the same problem to true FP64 relative residual 1e-8
+    (`names`: only these runs)."""
     import oracle as O
     bp = nb.BP(N_ORDER, n, n, n, perturb=0.1, seed=5)
     L = bp.Nlocal
@@ -321,6 +324,8 @@ def pcg_comparison(nb, torch, dev, n, learned):
         if net is not None:
             runs.append(("mixed_learned", dict(solver=nb.SOLVER_MIXED, inner_precision=nb.FP32,
                                                precond=nb.PRECOND_LEARNED, net=net)))
+    if names is not None:
+        runs = [rk for rk in runs if rk[0] in names]
     r, x = torch.empty_like(f), torch.empty_like(f)
     for name, kw in runs:
         # a 20-iteration warm-up on the same buffers instantiates the solver's
@@ -408,14 +413,16 @@ def nekbone_bp5(nb, torch, dev):
     return out
 
 
-def cpu_pcg_reference(pcg, n_gpu, seconds=2.0, n=16):
+def cpu_pcg_reference(pcg, n_gpu, seconds=2.0, n=16, gpu_same=None):
     """The reference's CPU path for the PCG (the oracle's OpenMP restatement:
-    CPU axhelm, gather-scatter and vector kernels as OpenMP loops over all host
-    threads) on a bounded sample of the same problem class as the GPU solves
-    (N=7 perturbed box, lambda0~U[0.5,1.5], lambda1~U[0.5,2.0], Dirichlet,
-    Jacobi): fixed FP64 iterations on E=n^3 elements, about `seconds` of CPU
-    work.  Its time to 1e-8 at the GPU's size is projected: the per-iteration
-    time scaled by the element ratio, times the GPU FP64 solve's iterations."""
+    the CPU baseline axhelm, gather-scatter and vector kernels as OpenMP loops
+    over all host threads) on the same problem class as the GPU solves (N=7
+    perturbed box, lambda0~U[0.5,1.5], lambda1~U[0.5,2.0], Dirichlet, Jacobi)
+    at E=n^3: fixed FP64 iterations (about `seconds` of CPU work) for the
+    per-iteration time, and one whole solve to 1e-8, measured, beside the GPU
+    solvers' measured times on the same problem (`gpu_same`).  The time to
+    1e-8 at the GPU's size is only projected: the per-iteration time scaled by
+    the element ratio, times the GPU FP64 solve's iterations."""
     import oracle as O
     m = O.BoxMesh(N_ORDER, n, n, n, perturb=0.1, seed=5)
     L = m.Nlocal
@@ -439,6 +446,17 @@ def cpu_pcg_reference(pcg, n_gpu, seconds=2.0, n=16):
            "seconds_per_iteration": per,
            "gdofs_per_iter": m.E * N_ORDER ** 3 / per / 1e9,
            "setup_s": setup}
+    r, x = f.copy(), np.zeros(L)
+    t0 = time.perf_counter()
+    it_full, setup_full = bp.pcg_omp(r, x, 1e-8, 20000)
+    full = time.perf_counter() - t0 - setup_full
+    out["measured_to_1e-8"] = {"E": m.E, "iterations": it_full, "seconds": full,
+                               "note": "whole CPU solve on all host threads, measured"}
+    if gpu_same:
+        out["measured_to_1e-8"]["gpu_same_problem"] = {
+            k2: {"iterations": v["iterations"], "seconds": v["elapsed_s"],
+                 "cpu_over_gpu": full / v["elapsed_s"]}
+            for k2, v in gpu_same.items() if isinstance(v, dict) and "elapsed_s" in v}
     fp64 = (pcg or {}).get("fp64_jacobi")
     if fp64:
         proj = per * (n_gpu ** 3 / m.E) * fp64["iterations"]
@@ -641,9 +659,11 @@ def run_gpu(args, rank, ws, local):
     del bp
     torch.cuda.empty_cache()
 
-    pcg = None
+    pcg = pcg_small = None
     if not args.no_pcg:
         pcg = pcg_comparison(nb, torch, dev, args.pcg_n, not args.no_learned)
+        pcg_small = pcg_comparison(nb, torch, dev, 16, False,
+                                   names=("fp64_jacobi", "fp64_split_jacobi", "mixed_fp32"))
     bp5 = None if args.no_pcg else nekbone_bp5(nb, torch, dev)
     net_cost = time_net(nb, torch, dev, E)
     for v in net_cost.values():
@@ -655,7 +675,8 @@ def run_gpu(args, rank, ws, local):
     cpu = CpuAxhelm().rate(args.cpu_seconds) if (rank == 0 and ws == 1) else None
     if pcg is not None and rank == 0 and ws == 1:
         try:
-            pcg["cpu_reference_fp64_jacobi"] = cpu_pcg_reference(pcg, args.pcg_n)
+            pcg["cpu_reference_fp64_jacobi"] = cpu_pcg_reference(pcg, args.pcg_n,
+                                                                 gpu_same=pcg_small)
         except Exception as exc:  # a failed baseline must not cost the bench line
             pcg["cpu_reference_fp64_jacobi"] = {"error": f"{type(exc).__name__}: {exc}"}
     if rank != 0:

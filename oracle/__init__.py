@@ -28,8 +28,8 @@ _vp = C.c_void_p
 
 
 def build(ref: bool = False) -> None:
-    """Compile liboracle.so (and the reference shims when ``ref``)."""
-    subprocess.run(["make", "-s", "-C", _HERE, "liboracle.so"], check=True)
+    """Compile liboracle.so and libcpuaxhelm.so (and the reference shims when ``ref``)."""
+    subprocess.run(["make", "-s", "-C", _HERE, "all"], check=True)
     if ref:
         subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=True)
 
@@ -70,6 +70,7 @@ def lib():
     L.nekbo_pcg.argtypes = [C.POINTER(NekboBP), _d, _d, C.c_double, C.c_int, C.c_int, C.c_int,
                             C.c_int, _vp]
     L.nekbo_bp_apply.argtypes = [C.POINTER(NekboBP), _d, _d]
+    L.nekbo_set_cpu_axhelm.argtypes = [C.c_void_p]
     L.nekbo_pcg_omp.restype = C.c_int
     L.nekbo_pcg_omp.argtypes = [C.POINTER(NekboBP), _d, _d, C.c_double, C.c_int, C.c_int, C.c_int,
                                 C.POINTER(C.c_double)]
@@ -234,8 +235,11 @@ class BP:
         return (it, h) if hist else it
 
     def pcg_omp(self, r, x, tol, maxit, precond=1, fixed=False):
-        """BPPCG on all host threads (the CPU timing baseline): returns
-        (iterations, set-up seconds)."""
+        """BPPCG on all host threads (the CPU timing baseline), its operator
+        from the CPU baseline build (cpu_axhelm.c): returns (iterations, set-up
+        seconds)."""
+        fn = C.cast(cpu_lib().nekbc_axhelm, C.c_void_p)
+        lib().nekbo_set_cpu_axhelm(fn)
         setup = C.c_double(0.0)
         it = lib().nekbo_pcg_omp(C.byref(self.s), r, x, tol, maxit, precond, int(fixed),
                                  C.byref(setup))
@@ -332,13 +336,43 @@ def net_loss_grad(Nq, W, x, t, C):
 
 
 # ----------------------------------------------------------------------------- reference shims
-def ref(Nq: int):
-    """The reference's own CPU axhelm compiled for this Nq, or None when not built."""
-    if Nq in _REFS:
-        return _REFS[Nq]
-    path = os.path.join(_HERE, "_ref", f"libnekref_nq{Nq}.so")
+_CPU = None
+
+
+def cpu_lib():
+    """The timed CPU baseline (cpu_axhelm.c): the reference's CPU axhelm with the
+    order fixed at compile time and the reference's -O3."""
+    global _CPU
+    if _CPU is None:
+        path = os.path.join(_HERE, "libcpuaxhelm.so")
+        if not os.path.exists(path):
+            build()
+        L = C.CDLL(path)
+        L.nekbc_axhelm.restype = C.c_int
+        L.nekbc_axhelm.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_int64, _d, _d, _vp, _d, _d]
+        _CPU = L
+    return _CPU
+
+
+def cpu_axhelm(Nq, bk, E, offset, ggeo, D, lam, q, Aq):
+    """Single-field axhelm on E elements with the CPU baseline (OpenMP)."""
+    lp = None if lam is None else np.ascontiguousarray(lam, dtype=np.float64)
+    rc = cpu_lib().nekbc_axhelm(Nq, int(bool(bk)), E, offset, ggeo, D,
+                                None if lp is None else lp.ctypes.data, q, Aq)
+    if rc != 0:
+        raise ValueError(f"CPU baseline: Nq={Nq} outside 2..14")
+    return Aq
+
+
+def ref(Nq: int, fast: bool = False):
+    """The reference's own CPU axhelm compiled for this Nq, or None when not
+    built; ``fast``: the build with the reference's own flags (make ref-fast)."""
+    key = (Nq, fast)
+    if key in _REFS:
+        return _REFS[key]
+    path = os.path.join(_HERE, "_ref", f"libnekref_{'fast_' if fast else ''}nq{Nq}.so")
     if not os.path.exists(path):
-        _REFS[Nq] = None
+        _REFS[key] = None
         return None
     L = C.CDLL(path)
     L.nekref_nq.restype = C.c_int
@@ -346,5 +380,5 @@ def ref(Nq: int):
     L.nekref_axhelm_cpu.restype = C.c_int
     L.nekref_axhelm_cpu.argtypes = [C.c_int, C.c_int, C.c_int, _d, _d, _vp, _d, _d]
     L.nekref_weighted_inner_product_update.argtypes = [C.c_int, C.c_int, _d, _d, _d, _d]
-    _REFS[Nq] = L
+    _REFS[key] = L
     return L

@@ -99,6 +99,11 @@ void nekbo_zero_mean(int64_t Nloc, int Nfields, int64_t offset, double* q);
 /* BPPCG on all host threads (OpenMP loops and reductions): the CPU timing
  * baseline of the PCG, not a parity reference.  *setup_s (nullable) receives
  * the time of the initial residual and the Jacobi set-up. */
+/* operator of the CPU baseline build (cpu_axhelm.c nekbc_axhelm): Nq, bk, E,
+ * offset, ggeo, D, lambda, q, Aq; returns 0 when it handled the call */
+typedef int (*nekbo_cpu_axhelm_fn)(int, int, int64_t, int64_t, const double*, const double*,
+                                   const double*, const double*, double*);
+void nekbo_set_cpu_axhelm(nekbo_cpu_axhelm_fn fn);
 int nekbo_pcg_omp(const nekbo_bp* bp, double* r, double* x, double tol, int maxit, int precond,
                   int fixed_iterations, double* setup_s);
 /* operator used by the PCG: Aq = mask(gs(axhelm(q))) */

@@ -284,3 +284,34 @@ def test_config1_e512_against_axhelm_reference(nb, O, dev):
         assert abs((got * got).sum() - float(g["Aq_sumsq"])) / float(g["Aq_sumsq"]) < 1e-12
         ref = O.axhelm(N + 1, E, L, nb.AX_BK, m.ggeo, m.D, np.zeros(2 * L), q)
         assert rel(got, ref) < 1e-12
+
+
+@pytest.mark.parametrize("N", [5, 7, 8])
+@pytest.mark.parametrize("flags", [0, 1, 2, 7])
+def test_fp64_any_derivative_matrix(nb, O, dev, N, flags):
+    """The FP64 kernel evaluates the even-odd form only for a centro-
+    antisymmetric D (nodes symmetric about the element centre); for any other
+    D it must evaluate the direct sums.  A random D, and a GLL D with one entry
+    moved by 1e-9, against the oracle at 1e-12."""
+    m = O.BoxMesh(N, 3, 2, 2, perturb=0.1, seed=60 + N)
+    E, L = m.E, m.Nlocal
+    nf = 3 if flags & nb.AX_N3 else 1
+    lam, q = fields(O, L, nf, 61 + N)
+    Drand = O.uniform((N + 1) ** 2, 62, N, -2, 2)
+    Dnudge = m.D.copy()
+    Dnudge[1] += 1e-9
+    for D in (Drand, Dnudge, m.D):
+        if flags & nb.AX_PARTIAL:
+            elist = np.arange(E - 1, -1, -2, dtype=np.int32)
+            ref = np.full(nf * L, 3.0)
+            O.axhelm(N + 1, len(elist), L, flags, m.ggeo, D, lam, q, element_list=elist, out=ref)
+            Aq = torch.full((nf * L,), 3.0, dtype=torch.float64, device=dev)
+            nb.axhelm(N + 1, flags, nb.FP64, len(elist), L, T(m.ggeo, dev), T(D, dev), T(lam, dev),
+                      T(q, dev), Aq, element_list=T(elist, dev))
+        else:
+            ref = O.axhelm(N + 1, E, L, flags, m.ggeo, D, lam, q)
+            Aq = torch.zeros(nf * L, dtype=torch.float64, device=dev)
+            nb.axhelm(N + 1, flags, nb.FP64, E, L, T(m.ggeo, dev), T(D, dev), T(lam, dev),
+                      T(q, dev), Aq)
+        torch.cuda.synchronize()
+        assert rel(Aq.cpu().numpy(), ref) < 1e-12

@@ -363,3 +363,27 @@ def test_bench_cpu_pcg_block_on_a_small_sample():
     assert out["projected_time_to_1e-8_s"] == pytest.approx(
         out["seconds_per_iteration"] * (8 ** 3 / 2 ** 3) * 100)
     assert set(out["gpu_speedup"]) == {"fp64_jacobi", "mixed_fp32"}
+
+
+@pytest.mark.parametrize("N", [1, 3, 7, 9, 13])
+def test_cpu_baseline_port_matches_checker(N):
+    """The timed CPU baseline (oracle/cpu_axhelm.c: the reference's CPU axhelm
+    with the order fixed at compile time and multiply-add fusion allowed)
+    agrees with the bit-identical checker to rounding, BK and Helmholtz; the
+    OpenMP PCG that uses it takes the checker PCG's iteration count."""
+    m = O.BoxMesh(N, 3, 2, 2, perturb=0.1, seed=70 + N)
+    E, L = m.E, m.Nlocal
+    q = O.uniform(L, N, 3, -1, 1)
+    lam = np.concatenate([O.uniform(L, N, 1, 0.5, 1.5), O.uniform(L, N, 2, 0.5, 2.0)])
+    for bk in (True, False):
+        got = O.cpu_axhelm(N + 1, bk, E, L, m.ggeo, m.D, None if bk else lam, q, np.zeros(L))
+        ref = O.axhelm(N + 1, E, L, O.AX_BK if bk else 0, m.ggeo, m.D, lam, q)
+        assert rel(got, ref) < 1e-14
+    if N == 7:
+        bp = O.BP(m, lam)
+        f = O.gs_many_add(bp.Ng, bp.offs, bp.gids, O.uniform(L, 5, 3, -1.0, 1.0))
+        f[m.maskIds] = 0.0
+        r1, x1, r2, x2 = f.copy(), np.zeros(L), f.copy(), np.zeros(L)
+        it_omp, _ = bp.pcg_omp(r1, x1, 1e-8, 2000)
+        it_chk = bp.pcg(r2, x2, 1e-8, 2000, precond=1)
+        assert abs(it_omp - it_chk) <= 1 and rel(x1, x2) < 1e-7
