@@ -5,6 +5,13 @@
  * checker the GPU library is compared against; the library never links it and
  * never falls back to it.  Compile with -ffp-contract=off so that x86 and Arm
  * hosts produce identical bits.
+ *
+ * Pinned to the reference itself: the axhelm loops to its compiled CPU
+ * kernels (kernel/CPU/axhelm.c, axhelmReference.cpp) and the weighted inner
+ * product to kernel/CPU/weightedInnerProduct.c (tests/golden/make_golden.py);
+ * gather-scatter, updateJacobi, the dot trees (v0, block) and adv at
+ * cubNq = Nq to the reference's OKL kernels run with OCCA's Serial semantics
+ * (oracle/okl_serial.py, tests/golden/make_okl_golden.py), bit for bit.
  */
 #include "nekb_oracle.h"
 

@@ -128,8 +128,9 @@ void nekbo_gelu_backward(int64_t n, const float* x, const float* gy, float* gx);
  * weightedInnerProduct2_v1 (dot.okl:114-169, its lockstep tree), 2
  * weightedBlockInnerProduct2 (dot.okl:67-111, Nfields triple products per
  * node).  Returns the number of blocks written, or -1 on bad arguments.
- * Parity unpinned: the kernels exist only as OKL (the OCCA runtime they need
- * builds only with CMake), so this is a restatement checked by its own tests. */
+ * Variants 0 and 2 are pinned bit for bit to the reference's OKL kernels run
+ * with OCCA's Serial semantics (tests/golden/okl_serial.npz); variant 1 only
+ * computes the right sum in lockstep, so it is checked by its total. */
 int64_t nekbo_dot_partials(int variant, int64_t N, int Nfields, int64_t offset, int blockSize,
                            const double* w, const double* x, const double* y, double* wxy);
 
@@ -138,8 +139,10 @@ int64_t nekbo_dot_partials(int variant, int64_t N, int Nfields, int64_t offset, 
  * Uc = (I x I x I) U, I(i <- a) = cubInterpT[a*cubNq + i]; metric slots of
  * core/params.h:2-13 (12 per node).  The t-projected slice is cubNq x cubNq
  * (the reference's s_U is Nq x Nq but indexed up to cubNq x cubNq,
- * adv.okl:203-231; the two agree for cubNq = Nq).  Parity unpinned, for the
- * same reason as the dot kernels; checked against exact polynomial answers. */
+ * adv.okl:203-231; the two agree for cubNq = Nq).  For cubNq = Nq pinned bit
+ * for bit to the reference's OKL kernel run with OCCA's Serial semantics
+ * (tests/golden/okl_serial.npz); for cubNq > Nq, where the reference's
+ * kernel runs past s_U, checked against exact polynomial answers. */
 void nekbo_adv_cubature(int Nq, int cubNq, int64_t Nelements, const double* vgeo,
                         const double* cubvgeo, const double* cubD, const double* cubInterpT,
                         int64_t offset, const double* U, double* NU);
