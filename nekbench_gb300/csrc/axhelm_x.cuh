@@ -276,7 +276,7 @@ int run(const AxArgs& a, cudaStream_t s)
   using C = CfgX<NQ, NF>;
   auto kern = k_axhelm_x<NQ, NF, BK>;
   static SmemOptIn smem_opt;
-  if (C::SMEM > 48 * 1024) NEKB_TRY(smem_opt.ensure(kern, C::SMEM));
+  NEKB_TRY(smem_opt.ensure(kern, C::SMEM));  // dynamic + static may pass 48 KB
   const int64_t nblk = (a.Nelements + C::NEL - 1) / C::NEL;
   if (nblk == 0) return NEKB_OK;
   if (nblk > INT_MAX) return fail(NEKB_ERR_INVALID, "axhelm: too many elements");

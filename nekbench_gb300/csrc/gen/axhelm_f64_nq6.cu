@@ -1,9 +1,9 @@
-// axhelm instantiation: precision NEKB_FP64, Nq=6.
-#include "../axhelm_impl.cuh"
+// axhelm instantiation: precision NEKB_FP64, Nq=6 (even-odd contractions).
+#include "../axhelm_eo.cuh"
 
 namespace nekb {
 int launch_axhelm_f64_nq6(int flags, const AxArgs& a, cudaStream_t s)
 {
-  return ax::run_flags<6, NEKB_FP64>(flags, a, s);
+  return ax_eo::run_flags<6>(flags, a, s);
 }
 }  // namespace nekb
