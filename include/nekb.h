@@ -327,13 +327,18 @@ int nekb_bp_pcg(nekb_bp* bp, const double* lambda, double* r, double* x, double 
  * No counterpart in the reference. */
 typedef struct nekb_net nekb_net;
 nekb_net* nekb_net_create(int Nq, int channels, int layers, uint64_t seed, int* status);
-/* inference arithmetic: NEKB_NET_TENSOR (default; BF16 tensor-core MMA with
- * BF16 activations between layers, FP32 sums; built for Nq=8 with 16
- * channels, other shapes fall back to NEKB_NET_FP32) or NEKB_NET_FP32 (FP32
- * activations and sums on the CUDA cores).  nekb_net_inference returns the
- * arithmetic actually used. */
-#define NEKB_NET_FP32   0
-#define NEKB_NET_TENSOR 1
+/* inference arithmetic: NEKB_NET_TENSOR (default: BF16 tensor-core MMAs with
+ * BF16 activations between layers and FP32 sums, on the library's preferred
+ * tensor-core kernel; built for Nq=8 with 16 channels, other shapes fall back
+ * to NEKB_NET_FP32), NEKB_NET_TENSOR_SYNC (that arithmetic on warp-level
+ * mma.sync instructions), NEKB_NET_TENSOR_TC5 (that arithmetic on tcgen05
+ * MMAs with accumulators in tensor memory) or NEKB_NET_FP32 (FP32 activations
+ * and sums on the CUDA cores).  nekb_net_inference returns the mode in use
+ * (NEKB_NET_FP32 where a tensor-core mode is not built for the shape). */
+#define NEKB_NET_FP32        0
+#define NEKB_NET_TENSOR      1
+#define NEKB_NET_TENSOR_SYNC 2
+#define NEKB_NET_TENSOR_TC5  3
 int nekb_net_set_inference(nekb_net* net, int mode);
 int nekb_net_inference(const nekb_net* net);
 void nekb_net_free(nekb_net* net);

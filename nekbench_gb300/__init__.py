@@ -29,7 +29,7 @@ FP64, FP32, BF16, FP32_TRILINEAR, FP64_SPLIT = 0, 1, 2, 3, 4
 DOUBLE, FLOAT = 0, 1
 PRECOND_COPY, PRECOND_JACOBI, PRECOND_LEARNED = 0, 1, 2
 SOLVER_FP64, SOLVER_MIXED, SOLVER_FP64_SPLIT = 0, 1, 2
-NET_FP32, NET_TENSOR = 0, 1
+NET_FP32, NET_TENSOR, NET_TENSOR_SYNC, NET_TENSOR_TC5 = 0, 1, 2, 3
 OK, ERR_INVALID, ERR_CUDA, ERR_ALLOC, ERR_UNSUPPORTED, ERR_BREAKDOWN, ERR_NOT_CONVERGED = \
     0, -1, -2, -3, -4, -5, -6
 
@@ -510,7 +510,8 @@ class Net:
 
     @property
     def inference(self):
-        """NET_TENSOR (BF16 tensor-core MMA) or NET_FP32 (CUDA cores), as used."""
+        """NET_TENSOR (BF16 tensor-core MMAs, the library's kernel), NET_TENSOR_SYNC
+        (mma.sync), NET_TENSOR_TC5 (tcgen05) or NET_FP32 (CUDA cores), as used."""
         return check_value(lib().nekb_net_inference(self.h))
 
     @inference.setter

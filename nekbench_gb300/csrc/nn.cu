@@ -589,10 +589,17 @@ int run_train(nekb_net* net, int64_t E, const float* in, const float* target, cu
   }                                                                         \
   return fail(NEKB_ERR_UNSUPPORTED, "net: Nq=%d C=%d not built (Nq 4/6/8, C 4/8/16)", net->Nq, net->C);
 
+// the tensor-core kernel NEKB_NET_TENSOR selects
+constexpr int kTensorDefault = NEKB_NET_TENSOR_SYNC;
+
 int net_infer(const nekb_net* net, int64_t Etot, int64_t Efield, const float* r, const float* w,
               const float* invDiag, float* out, int normalize, const int* skip, cudaStream_t s)
 {
-  if (net->inference == NEKB_NET_TENSOR && net_tc_supported(net->Nq, net->C))
+  const int mode = net->inference == NEKB_NET_TENSOR ? kTensorDefault : net->inference;
+  if (mode == NEKB_NET_TENSOR_TC5 && net_tc_supported(net->Nq, net->C))
+    return net_infer_tc5(net->Wbf.as<__nv_bfloat16>(), Etot, Efield, r, w, invDiag, out, normalize,
+                         skip, s);
+  if (mode == NEKB_NET_TENSOR_SYNC && net_tc_supported(net->Nq, net->C))
     return net_infer_tc(net->Wbf.as<__nv_bfloat16>(), Etot, Efield, r, w, invDiag, out, normalize,
                         skip, s);
   NEKB_NET_DISPATCH(run_infer, net, Etot, Efield, r, w, invDiag, out, normalize, skip, s)
@@ -712,7 +719,7 @@ void nekb_net_free(nekb_net* net) { delete net; }
 
 int nekb_net_set_inference(nekb_net* net, int mode)
 {
-  if (!net || (mode != NEKB_NET_FP32 && mode != NEKB_NET_TENSOR))
+  if (!net || mode < NEKB_NET_FP32 || mode > NEKB_NET_TENSOR_TC5)
     return fail(NEKB_ERR_INVALID, "net inference: bad handle or mode %d", mode);
   net->inference = mode;
   return NEKB_OK;
@@ -721,8 +728,8 @@ int nekb_net_set_inference(nekb_net* net, int mode)
 int nekb_net_inference(const nekb_net* net)
 {
   if (!net) return fail(NEKB_ERR_INVALID, "net inference: NULL handle");
-  return (net->inference == NEKB_NET_TENSOR && net_tc_supported(net->Nq, net->C)) ? NEKB_NET_TENSOR
-                                                                                  : NEKB_NET_FP32;
+  if (net->inference != NEKB_NET_FP32 && net_tc_supported(net->Nq, net->C)) return net->inference;
+  return NEKB_NET_FP32;
 }
 
 int nekb_net_num_params(const nekb_net* net) { return net ? net->P : 0; }
@@ -748,7 +755,7 @@ int nekb_net_forward(nekb_net* net, int64_t E, const float* in, float* out, void
   if (E == 0) return NEKB_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   NEKB_TRY(net_infer(net, E, E, in, nullptr, nullptr, out, 0, nullptr, s));
-  if (nekb_net_inference(net) == NEKB_NET_TENSOR) {
+  if (nekb_net_inference(net) != NEKB_NET_FP32) {
     NEKB_CUDA(cudaStreamSynchronize(s));
     return net_tc_copy_timeout();
   }

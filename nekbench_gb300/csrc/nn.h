@@ -17,16 +17,22 @@ int net_precondition(nekb_bp* bp, nekb_net* net, const float* r, float* z, const
 // w invDiag r to the output
 constexpr int kNetNormalize = 1, kNetAddJacobi = 2;
 
-// tensor-core inference (nn_tc.cu): Nq=8, 16 channels
+// tensor-core inference, Nq=8, 16 channels: tcgen05 MMAs with TMEM
+// accumulators (nn_tc5.cu) and warp-level mma.sync (nn_tc.cu)
 bool net_tc_supported(int Nq, int C);
+int net_infer_tc5(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const float* r,
+                  const float* w, const float* invDiag, float* out, int normalize, const int* skip,
+                  cudaStream_t s);
 int net_infer_tc(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const float* r,
                  const float* w, const float* invDiag, float* out, int normalize, const int* skip,
                  cudaStream_t s);
-// NEKB_OK, or an error (and the flag cleared) when a tensor-core launch gave up
-// waiting for its input copies since the last call
+// NEKB_OK, or an error (and the flags cleared) when a tensor-core launch gave
+// up waiting for its input copies or its MMAs since the last call
 int net_tc_copy_timeout();
-// sets the timeout flag from the host, as the kernel does when an input copy
-// does not complete (for tests of the error path; no device wait runs out)
+// sets the timeout flags from the host, as the kernels do when a wait runs out
+// (for tests of the error path; no device wait runs out)
 int net_tc_raise_copy_timeout();
+int net_tc5_take_timeout(int* flag);
+int net_tc5_raise_timeout();
 
 }  // namespace nekb

@@ -1,6 +1,7 @@
-// Tensor-core inference of the learned element preconditioner for N=7 (Nq=8,
-// 512 nodes) and 16 channels: the three 3x3x3 convolutions of an element as
-// implicit GEMMs on the BF16 tensor cores (mma.m16n8k16, FP32 accumulation).
+// Warp-level tensor-core inference of the learned element preconditioner for
+// N=7 (Nq=8, 512 nodes) and 16 channels (NEKB_NET_TENSOR_SYNC; nn_tc5.cu holds
+// the tcgen05 kernel): the three 3x3x3 convolutions of an element as implicit
+// GEMMs on the BF16 tensor cores (mma.m16n8k16, FP32 accumulation).
 //
 // One CTA of 4 warps per element at a time (persistent grid).  Node n =
 // i + 8j + 64k; warp w owns the 16 nodes j in {2w, 2w+1}, i = 0..7 of every
@@ -398,13 +399,15 @@ k_net_infer_tc(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ W
 
 int net_tc_copy_timeout()
 {
-  int flag = 0;
+  int flag = 0, flag5 = 0;
   NEKB_CUDA(cudaMemcpyFromSymbol(&flag, g_tc_copy_timeout, sizeof(int)));
   if (flag) {
     const int zero = 0;
     NEKB_CUDA(cudaMemcpyToSymbol(g_tc_copy_timeout, &zero, sizeof(int)));
-    return fail(NEKB_ERR_CUDA, "network: an input copy did not complete in time");
   }
+  NEKB_TRY(net_tc5_take_timeout(&flag5));
+  if (flag || flag5)
+    return fail(NEKB_ERR_CUDA, "network: an input copy or a tensor-core operation did not complete in time");
   return NEKB_OK;
 }
 
@@ -412,7 +415,7 @@ int net_tc_raise_copy_timeout()
 {
   const int one = 1;
   NEKB_CUDA(cudaMemcpyToSymbol(g_tc_copy_timeout, &one, sizeof(int)));
-  return NEKB_OK;
+  return net_tc5_raise_timeout();
 }
 
 bool net_tc_supported(int Nq, int C) { return Nq == kNq && C == 16; }

@@ -1,0 +1,514 @@
+// Learned element preconditioner for N=7 (Nq=8, 512 nodes), 16 channels, on
+// the fifth-generation tensor cores: tcgen05.mma with operands in shared
+// memory and accumulators in tensor memory (TMEM).
+//
+// Layout.  An element's nodes (i, j, k) are stored with one zero row of nodes
+// before and after every j line-set and one zero plane before and after the
+// k planes: padded row n' = i + 8 j' + 80 k', j' = j + 1 in 0..9, k' = k + 1
+// in 0..9 (800 rows, plus 8 spare rows at both ends).  Activations are BF16,
+// [row][16 channels], in the canonical no-swizzle K-major layout of core
+// matrices (8 rows x 16 bytes): row group g = row/8, channel half h = c/8 at
+// byte (2 g + h) * 128.  A shift of the input by (dj, dk) is then a shift of
+// the A operand's start address by (8 dj + 80 dk) rows, i.e. whole row groups,
+// and the padding supplies the zeros outside the element.
+//
+// Layer 2 (16 -> 16) as one GEMM per 128-row tile (5 tiles cover planes
+// k = 0..7): K runs over (dj, dk, ci) -- nine MMAs of K = 16, one per shifted
+// A -- and N over (di, co) = 48 columns:
+//   V[n'][di][co] = sum_{dj,dk,ci} act[n' + 8 dj + 80 dk][ci] W[(di,dj,dk)][ci][co].
+// The di shift is left to the epilogue: out(i) = sum_di V(i + di)[di], and
+// node i +- 1 is lane +- 1 of the same warp (tile rows start at multiples of 8,
+// so lane mod 8 = i), so two shuffles finish the convolution.  Layer 1
+// (1 -> 16) uses an im2col of the 9 (di, dk) taps as its 16-wide K (three MMAs
+// for dj = -1, 0, 1, N = 16) and layer 3 (16 -> 1) the layer-2 scheme with
+// N = 16 (columns di = -1, 0, 1 used).  Every TMEM read-back stays in the
+// reading warp's own 32 lanes: no shared-memory round trip of the partial sums.
+//
+// One CTA of 4 warps per element at a time (persistent grid, two CTAs per SM,
+// 256 TMEM columns each: layer 2 holds 5 x 48).  Thread 0 issues the MMAs of a
+// layer tile by tile and commits each tile to its own mbarrier, so the
+// epilogue of tile t (TMEM -> registers, shuffles, GELU, BF16, next layer's
+// operand) overlaps the MMAs of the later tiles.  The next element's input
+// rows arrive by bulk asynchronous copies meanwhile.  Every wait is bounded;
+// a wait that runs out sets a device flag, the CTA waits (bounded) for its
+// operations in flight, frees its TMEM and returns.
+//
+// Arithmetic: BF16 weights and activations (the scaled input and both GELU
+// outputs rounded to BF16), FP32 accumulation, the tanh form of GELU with the
+// hardware tanh.  No counterpart in the reference.
+#include "nn.h"
+
+#include <cuda_bf16.h>
+
+namespace nekb {
+namespace {
+
+constexpr int kNq = 8, kNp = 512, kTaps = 27, kThreads = 128;
+constexpr int kO2 = kTaps * 16, kO3 = kTaps * 16 + kTaps * 16 * 16;
+constexpr int kPlaneRows = 80;           // 8 i x 10 j' per padded plane
+constexpr int kLead = 8;                 // spare rows before padded row 0
+constexpr int kRows = 816;               // 8 + 800 + 8 storage rows
+constexpr int kTiles = 5;                // 128-row tiles over padded rows 80..719
+constexpr int kTile0 = kPlaneRows;       // first tile row (plane k' = 1)
+constexpr int kActBytes = kRows * 32;    // one activation buffer
+
+// shared memory (bytes)
+constexpr int kSmW1 = 0;                         // 3 x [16 n][16 k] bf16
+constexpr int kSmW2 = kSmW1 + 3 * 512;           // 9 x [48 n][16 k]
+constexpr int kSmW3 = kSmW2 + 9 * 1536;          // 9 x [16 n][16 k]
+constexpr int kSmX = 20480;                      // layer-1 im2col, then layer-2 output
+constexpr int kSmY = kSmX + kActBytes + 512;     // layer-1 output (47104)
+constexpr int kSmIn = kSmY + kActBytes;          // [2 buffers][r, invDiag, w][512] floats
+constexpr int kSmH = kSmIn + 2 * 3 * kNp * 4;    // sqrt(invDiag), 512 floats
+constexpr int kSmA0 = kSmH + kNp * 4;            // scaled input (BF16 values), 512 floats
+constexpr int kSmRed = kSmA0 + kNp * 4;          // block sums
+constexpr int kSmBar = kSmRed + 64;              // 2 input + 5 tile mbarriers
+constexpr int kSmSlot = kSmBar + 8 * 8;          // TMEM base address
+constexpr int kSmTotal = kSmSlot + 16;
+constexpr int kRowBytes = kNp * 4;
+constexpr uint32_t kTmemCols = 256;
+constexpr long kWaitLimit = 1L << 22;
+
+static_assert(kSmX % 1024 == 0 && kSmY % 256 == 0, "operand buffers aligned");
+static_assert(kSmTotal * 3 > 227 * 1024, "at most two CTAs per SM share the 512 TMEM columns");
+
+// set when a wait (input copy or MMA) did not complete within kWaitLimit polls
+__device__ int g_tc5_timeout;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p)
+{
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// byte offset of (row, channel half) in an operand buffer
+__device__ __forceinline__ int core_off(int row, int half) { return ((row >> 3) * 2 + half) * 128 + (row & 7) * 16; }
+
+// shared-memory matrix descriptor: no swizzle, K-major; leading (K) byte
+// offset 128 between the two 8-wide channel halves, stride byte offset 256
+// between consecutive 8-row groups
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr)
+{
+  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) |
+         ((uint64_t)1 << 46);
+}
+
+// instruction descriptor: BF16 x BF16 -> FP32, both K-major, M = 128
+__host__ __device__ constexpr uint32_t idesc_n(int N)
+{
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t id, uint32_t acc)
+{
+  asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+               " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+               "l"(a), "l"(b), "r"(id), "r"(acc)
+               : "memory");
+}
+
+__device__ __forceinline__ void commit(uint32_t bar)
+{
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16])
+{
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+        "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int c = 0; c < 16; ++c) v[c] = __uint_as_float(r[c]);
+}
+
+__device__ __forceinline__ void ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ uint32_t pack2(float lo, float hi)
+{
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+__device__ __forceinline__ float gelu_tc(float x)
+{
+  const float u = 0.7978845608028654f * (x + 0.044715f * x * x * x);
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
+  return 0.5f * x * (1.0f + t);
+}
+
+// 16 channels of one row into an operand buffer (two 16-byte stores)
+__device__ __forceinline__ void store_row(unsigned char* buf, int row, const float (&v)[16])
+{
+  uint4 lo, hi;
+  lo.x = pack2(v[0], v[1]);
+  lo.y = pack2(v[2], v[3]);
+  lo.z = pack2(v[4], v[5]);
+  lo.w = pack2(v[6], v[7]);
+  hi.x = pack2(v[8], v[9]);
+  hi.y = pack2(v[10], v[11]);
+  hi.z = pack2(v[12], v[13]);
+  hi.w = pack2(v[14], v[15]);
+  *reinterpret_cast<uint4*>(buf + core_off(row, 0)) = lo;
+  *reinterpret_cast<uint4*>(buf + core_off(row, 1)) = hi;
+}
+
+__device__ __forceinline__ void bar_init(uint32_t bar)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void bar_expect(uint32_t bar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void bulk_row(uint32_t dst, const float* src, uint32_t bar)
+{
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+      "l"(src), "r"((uint32_t)kRowBytes), "r"(bar)
+      : "memory");
+}
+
+// true once the barrier has completed the phase with the given parity; false
+// after kWaitLimit polls
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity)
+{
+  for (long it = 0; it < kWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ float block_sum4(float v, float* red)
+{
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  return red[0] + red[1] + red[2] + red[3];
+}
+
+// B operands, [n][k] K-major in core matrices: element (n, k) at
+// ((n/8)*2 + k/8)*128 + (n%8)*16 + (k%8)*2
+__device__ __forceinline__ int wb_off(int n, int k) { return ((n >> 3) * 2 + (k >> 3)) * 128 + (n & 7) * 16 + (k & 7) * 2; }
+
+__global__ void __launch_bounds__(kThreads, 2)
+k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ Wbf,
+                const float* __restrict__ r, const float* __restrict__ w, const float* __restrict__ invDiag,
+                float* __restrict__ out, int normalize, const int* skip)
+{
+  if (skip != nullptr && *skip != 0) return;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  unsigned char* X = smem + kSmX;
+  unsigned char* Y = smem + kSmY;
+  float* hs = reinterpret_cast<float*>(smem + kSmH);
+  float* a0 = reinterpret_cast<float*>(smem + kSmA0);
+  float* red = reinterpret_cast<float*>(smem + kSmRed);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint16_t* W = reinterpret_cast<const uint16_t*>(Wbf);
+  const uint32_t bar_in = smem_addr(smem + kSmBar), bar_t = bar_in + 16;
+  const uint32_t sW1 = smem_addr(smem + kSmW1), sW2 = smem_addr(smem + kSmW2), sW3 = smem_addr(smem + kSmW3);
+  const uint32_t sX = smem_addr(X), sY = smem_addr(Y);
+
+  // ---- weights as B operands (once per CTA); both activation buffers zeroed
+  // (their padding rows are never written again)
+  for (int x = tid; x < 3 * 16 * 16; x += kThreads) {  // W1[dj][co][c], c = (di+1) + 3 (dk+1)
+    const int a = x / 256, co = (x / 16) % 16, c = x % 16;
+    uint16_t v = 0;
+    if (c < 9) {
+      const int t = (c % 3) + 3 * a + 9 * (c / 3);
+      v = W[co * kTaps + t];
+    }
+    *reinterpret_cast<uint16_t*>(smem + kSmW1 + a * 512 + wb_off(co, c)) = v;
+  }
+  for (int x = tid; x < 9 * 48 * 16; x += kThreads) {  // W2[(dj,dk)][(di,co)][ci]
+    const int b = x / 768, n = (x / 16) % 48, ci = x % 16;
+    const int dj = b % 3, dk = b / 3, di = n / 16, co = n % 16;
+    const int t = di + 3 * dj + 9 * dk;
+    *reinterpret_cast<uint16_t*>(smem + kSmW2 + b * 1536 + wb_off(n, ci)) = W[kO2 + (co * 16 + ci) * kTaps + t];
+  }
+  for (int x = tid; x < 9 * 16 * 16; x += kThreads) {  // W3[(dj,dk)][di][ci], di columns 0..2
+    const int b = x / 256, n = (x / 16) % 16, ci = x % 16;
+    const int dj = b % 3, dk = b / 3;
+    uint16_t v = 0;
+    if (n < 3) v = W[kO3 + ci * kTaps + n + 3 * dj + 9 * dk];
+    *reinterpret_cast<uint16_t*>(smem + kSmW3 + b * 512 + wb_off(n, ci)) = v;
+  }
+  for (int x = tid; x < kActBytes / 16; x += kThreads) {
+    reinterpret_cast<uint4*>(X)[x] = make_uint4(0, 0, 0, 0);
+    reinterpret_cast<uint4*>(Y)[x] = make_uint4(0, 0, 0, 0);
+  }
+  if (tid == 0) {
+    for (int b = 0; b < 2 + kTiles; ++b) bar_init(bar_in + 8 * b);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  fence_async_smem();
+  uint32_t* slot = reinterpret_cast<uint32_t*>(smem + kSmSlot);
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(slot)),
+                 "r"(kTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = *slot;
+  const uint32_t tlane = tmem + ((uint32_t)(32 * warp) << 16);  // this warp's TMEM lanes
+
+  // input rows r, invDiag, w of an element, double-buffered, by bulk copies
+  const float* inb = reinterpret_cast<const float*>(smem + kSmIn);
+  const uint32_t in_s = smem_addr(smem + kSmIn);
+  const uint32_t nrows = 1u + (invDiag ? 1u : 0u) + (w ? 1u : 0u);
+  auto fetch = [&](int64_t el, int buf) {
+    const uint32_t bar = bar_in + 8 * buf, dst = in_s + buf * 3 * kRowBytes;
+    bar_expect(bar, nrows * kRowBytes);
+    bulk_row(dst, r + el * kNp, bar);
+    if (invDiag) bulk_row(dst + kRowBytes, invDiag + (el % Efield) * kNp, bar);
+    if (w) bulk_row(dst + 2 * kRowBytes, w + (el % Efield) * kNp, bar);
+  };
+  if (tid == 0 && (int64_t)blockIdx.x < Etot) fetch(blockIdx.x, 0);
+  uint32_t pin[2] = {0u, 0u};
+  uint32_t tphase = 0;  // completed phases of every tile barrier
+  int buf = 0;
+  bool failed = false, input_failed = false, copy_pending = false;
+  const int i = lane & 7;  // node i of this thread's rows (tile rows start at multiples of 8)
+
+  // issue the MMAs of one layer: tile t accumulates nmat K=16 products into
+  // TMEM columns ncol * t onwards, then commits to its barrier
+  auto issue = [&](uint32_t sA, uint32_t sB, int bstride, int nmat, int ncol, uint32_t id, bool l1) {
+    if (tid != 0) return;
+    fence_after();
+#pragma unroll 1
+    for (int t = 0; t < kTiles; ++t) {
+      for (int b = 0; b < nmat; ++b) {
+        const int dj = l1 ? b - 1 : b % 3 - 1, dk = l1 ? 0 : b / 3 - 1;
+        const int row0 = kLead + kTile0 + 128 * t + 8 * dj + kPlaneRows * dk;
+        mma(tmem + (uint32_t)(ncol * t), sdesc(sA + (uint32_t)(row0 / 8) * 256),
+            sdesc(sB + (uint32_t)(b * bstride)), id, b > 0 ? 1u : 0u);
+      }
+      commit(bar_t + 8 * t);
+    }
+  };
+  auto wait_tile = [&](int t) -> bool {
+    const bool ok = bar_wait(bar_t + 8 * t, tphase & 1u);
+    fence_after();
+    return ok;
+  };
+
+  for (int64_t e = blockIdx.x; e < Etot; e += gridDim.x, buf ^= 1) {
+    const bool next = e + gridDim.x < Etot;
+    if (tid == 0 && next) {
+      fence_async_smem();  // the other buffer's reads are done
+      fetch(e + gridDim.x, buf ^ 1);
+    }
+    copy_pending = next;
+    const bool okin = bar_wait(bar_in + 8 * buf, pin[buf]);
+    pin[buf] ^= 1u;
+    if (__syncthreads_or(!okin)) { failed = true; input_failed = true; break; }
+    const float* rin = inb + buf * 3 * kNp;
+    const float* din = rin + kNp;
+    const float* win = rin + 2 * kNp;
+
+    // ---- scaled input a0 = bf16(h r / s)
+    float ss = 0.f;
+#pragma unroll
+    for (int c = 0; c < kNp / kThreads; ++c) {
+      const int n = tid + c * kThreads;
+      const float h = invDiag ? sqrtf(din[n]) : 1.f;
+      const float v = h * rin[n];
+      hs[n] = h;
+      a0[n] = v;
+      ss += v * v;
+    }
+    float s = 1.f;
+    if (normalize & kNetNormalize) s = sqrtf(block_sum4(ss, red) / kNp);
+    const float inv = s > 0.f ? 1.f / s : 0.f;
+#pragma unroll
+    for (int c = 0; c < kNp / kThreads; ++c) {
+      const int n = tid + c * kThreads;
+      a0[n] = __bfloat162float(__float2bfloat16_rn(a0[n] * inv));
+    }
+    __syncthreads();
+
+    // ---- layer-1 operand in X: row (i, j', k') holds the 9 inputs at
+    // (i + di, j' - 1, k' - 1 + dk), column (di + 1) + 3 (dk + 1); rows outside
+    // planes k' = 1..8 stay zero (they are layer 3's zero padding)
+    for (int rs = tid; rs < kRows; rs += kThreads) {
+      const int np = rs - kLead;
+      float v[16];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) v[c] = 0.f;
+      if (np >= kTile0 && np < kTile0 + kTiles * 128) {
+        const int ii = np & 7, jj = ((np >> 3) % 10) - 1, kk = np / kPlaneRows - 1;
+        if (jj >= 0 && jj < kNq) {
+#pragma unroll
+          for (int c = 0; c < 9; ++c) {
+            const int di = c % 3 - 1, dk = c / 3 - 1;
+            const int a = ii + di, b = kk + dk;
+            if (a >= 0 && a < kNq && b >= 0 && b < kNq) v[c] = a0[a + kNq * jj + kNq * kNq * b];
+          }
+        }
+      }
+      store_row(X, rs, v);
+    }
+    fence_async_smem();
+    fence_before();
+    __syncthreads();
+
+    // ---- layer 1: 1 -> 16, GELU, into Y
+    issue(sX, sW1, 512, 3, 16, idesc_n(16), true);
+    bool ok = true;
+#pragma unroll 1
+    for (int t = 0; t < kTiles; ++t) {
+      ok = wait_tile(t) && ok;
+      float v[16];
+      ld16(tlane + (uint32_t)(16 * t), v);
+      ld_wait();
+      const int np = kTile0 + 128 * t + 32 * warp + lane;
+      const int jp = (np >> 3) % 10;
+      const bool live = jp >= 1 && jp <= kNq;
+#pragma unroll
+      for (int c = 0; c < 16; ++c) v[c] = live ? gelu_tc(v[c]) : 0.f;
+      store_row(Y, np + kLead, v);
+    }
+    ++tphase;
+    fence_async_smem();
+    fence_before();
+    if (__syncthreads_or(!ok)) { failed = true; break; }
+
+    // ---- layer 2: 16 -> 16, GELU, into X
+    issue(sY, sW2, 1536, 9, 48, idesc_n(48), false);
+#pragma unroll 1
+    for (int t = 0; t < kTiles; ++t) {
+      ok = wait_tile(t) && ok;
+      float vm[16], v0[16], vp[16];
+      ld16(tlane + (uint32_t)(48 * t), vm);
+      ld16(tlane + (uint32_t)(48 * t + 16), v0);
+      ld16(tlane + (uint32_t)(48 * t + 32), vp);
+      ld_wait();
+      const int np = kTile0 + 128 * t + 32 * warp + lane;
+      const int jp = (np >> 3) % 10;
+      const bool live = jp >= 1 && jp <= kNq;
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        const float up = __shfl_down_sync(0xffffffffu, vp[c], 1);  // node i + 1, column di = +1
+        const float dn = __shfl_up_sync(0xffffffffu, vm[c], 1);    // node i - 1, column di = -1
+        float o = v0[c];
+        if (i < kNq - 1) o += up;
+        if (i > 0) o += dn;
+        v0[c] = live ? gelu_tc(o) : 0.f;
+      }
+      store_row(X, np + kLead, v0);
+    }
+    ++tphase;
+    fence_async_smem();
+    fence_before();
+    if (__syncthreads_or(!ok)) { failed = true; break; }
+
+    // ---- layer 3: 16 -> 1 and the output
+    issue(sX, sW3, 512, 9, 16, idesc_n(16), false);
+#pragma unroll 1
+    for (int t = 0; t < kTiles; ++t) {
+      ok = wait_tile(t) && ok;
+      float v[16];
+      ld16(tlane + (uint32_t)(16 * t), v);
+      ld_wait();
+      const float up = __shfl_down_sync(0xffffffffu, v[2], 1);
+      const float dn = __shfl_up_sync(0xffffffffu, v[0], 1);
+      float o = v[1];
+      if (i < kNq - 1) o += up;
+      if (i > 0) o += dn;
+      const int np = kTile0 + 128 * t + 32 * warp + lane;
+      const int jp = (np >> 3) % 10, kp = np / kPlaneRows;
+      if (jp >= 1 && jp <= kNq) {
+        const int n = i + kNq * (jp - 1) + kNq * kNq * (kp - 1);
+        o *= hs[n] * s;
+        if ((normalize & kNetAddJacobi) && invDiag) o += din[n] * rin[n];
+        out[e * kNp + n] = (w ? win[n] : 1.f) * o;
+      }
+    }
+    ++tphase;
+    fence_before();
+    if (__syncthreads_or(!ok)) { failed = true; break; }
+  }
+
+  if (failed) {  // flag, then wait (bounded) for this CTA's operations in flight
+    if (tid == 0) {
+      atomicExch(&g_tc5_timeout, 1);
+      if (input_failed) {
+        bar_wait(bar_in + 8 * buf, pin[buf] ^ 1u);  // the copy that did not arrive
+      } else {
+        for (int t = 0; t < kTiles; ++t) bar_wait(bar_t + 8 * t, tphase & 1u);
+      }
+      if (copy_pending) bar_wait(bar_in + 8 * (buf ^ 1), pin[buf ^ 1]);
+    }
+    fence_before();
+    __syncthreads();
+  }
+  fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
+}
+
+}  // namespace
+
+// reads and clears the timeout flag
+int net_tc5_take_timeout(int* flag)
+{
+  NEKB_CUDA(cudaMemcpyFromSymbol(flag, g_tc5_timeout, sizeof(int)));
+  if (*flag) {
+    const int zero = 0;
+    NEKB_CUDA(cudaMemcpyToSymbol(g_tc5_timeout, &zero, sizeof(int)));
+  }
+  return NEKB_OK;
+}
+
+int net_tc5_raise_timeout()
+{
+  const int one = 1;
+  NEKB_CUDA(cudaMemcpyToSymbol(g_tc5_timeout, &one, sizeof(int)));
+  return NEKB_OK;
+}
+
+int net_infer_tc5(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const float* r, const float* w,
+                  const float* invDiag, float* out, int normalize, const int* skip, cudaStream_t s)
+{
+  for (const void* p : {(const void*)r, (const void*)w, (const void*)invDiag})
+    if (reinterpret_cast<uintptr_t>(p) % 16 != 0)
+      return fail(NEKB_ERR_INVALID, "network: input arrays must be 16-byte aligned");
+  static SmemOptIn smem_opt;
+  NEKB_TRY(smem_opt.ensure(k_net_infer_tc5, kSmTotal));
+  int dev = 0, sms = 152, per_sm = 0;
+  NEKB_CUDA(cudaGetDevice(&dev));
+  NEKB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  NEKB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_net_infer_tc5, kThreads, kSmTotal));
+  if (per_sm < 1) per_sm = 1;
+  if (per_sm > 2) per_sm = 2;  // 2 x 256 TMEM columns per SM
+  int64_t grid = (int64_t)sms * per_sm;
+  if (grid > Etot) grid = Etot;
+  if (grid < 1) return NEKB_OK;
+  k_net_infer_tc5<<<(unsigned)grid, kThreads, kSmTotal, s>>>(Etot, Efield, Wbf, r, w, invDiag, out,
+                                                              normalize, skip);
+  NEKB_CUDA(cudaGetLastError());
+  return NEKB_OK;
+}
+
+}  // namespace nekb

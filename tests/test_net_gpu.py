@@ -151,11 +151,18 @@ def test_local_correction_is_the_element_interior_solve(nb, O, dev, N):
     assert np.all(got[-1] == 0.0)
 
 
+@pytest.mark.parametrize("mode", ["NET_TENSOR", "NET_TENSOR_SYNC", "NET_TENSOR_TC5"])
 @pytest.mark.parametrize("seed", [3, 4])
-def test_tensor_core_forward_matches_oracle(nb, O, dev, seed):
+def test_tensor_core_forward_matches_oracle(nb, O, dev, seed, mode):
+    """Every tensor-core kernel (the default, warp-level mma.sync, and tcgen05
+    with accumulators in tensor memory) against the oracle's convolutions on
+    BF16-rounded weights and activations; E = 37 elements, so the persistent
+    grid's CTAs take different element counts."""
     Nq, C, E = 8, 16, 37
     net = nb.Net(Nq, C, 3, seed=seed)
     assert net.inference == nb.NET_TENSOR
+    net.inference = getattr(nb, mode)
+    assert net.inference == getattr(nb, mode)
     W = bf16(net.weights())
     x = O.uniform(E * Nq ** 3, 40 + seed, 1, -1, 1).astype(np.float32)
     out = torch.zeros(E * Nq ** 3, dtype=torch.float32, device=dev)
@@ -168,6 +175,49 @@ def test_tensor_core_forward_matches_oracle(nb, O, dev, seed):
     d = out.cpu().numpy().astype(np.float64) - ref
     assert np.abs(d).max() <= 1e-2 * np.abs(ref).max()
     assert np.sqrt(np.mean(d * d)) <= 2e-3 * np.sqrt(np.mean(ref * ref))
+
+
+def test_tensor_core_kernels_agree_on_many_elements(nb, O, dev):
+    """tcgen05 and mma.sync inference on 3000 elements (each CTA of the
+    persistent grids loops over several elements), with the solver's input
+    scaling, Jacobi term and weights: the same BF16 arithmetic in different
+    summation orders, so the outputs agree to a few BF16 steps of the
+    activations."""
+    net = nb.Net(8, 16, 3, seed=9)
+    E = 3000
+    x = torch.from_numpy(O.uniform(E * 512, 77, 1, -1, 1).astype(np.float32)).to(dev)
+    outs = []
+    for mode in (nb.NET_TENSOR_TC5, nb.NET_TENSOR_SYNC):
+        net.inference = mode
+        o = torch.zeros_like(x)
+        net.forward(x, o, E)
+        outs.append(o)
+    torch.cuda.synchronize()
+    d = (outs[0] - outs[1]).double()
+    ref = outs[1].double()
+    assert float(d.abs().max()) <= 1e-2 * float(ref.abs().max())
+    assert float(d.pow(2).mean().sqrt()) <= 2e-3 * float(ref.pow(2).mean().sqrt())
+
+
+def test_learned_solve_on_tcgen05_kernel(nb, O, dev):
+    """Flexible CG with the network evaluated by the tcgen05 kernel reaches the
+    FP64 tolerance and takes about the iterations of the mma.sync kernel."""
+    bp = nb.BP(7, 6, 6, 6, perturb=0.1, seed=3)
+    L = bp.Nlocal
+    lam = torch.cat([torch.full((L,), 1.0), torch.full((L,), 1.5)]).double().to(dev)
+    f = torch.from_numpy(O.uniform(L, 8, 3, -1, 1)).to(dev)
+    bp.ogs.gather_scatter_many(f)
+    net = nb.Net.load(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                   "nekbench_gb300", "weights", "precond_n7_c16.bin"))
+    its = {}
+    for mode in (nb.NET_TENSOR_TC5, nb.NET_TENSOR_SYNC):
+        net.inference = mode
+        r, x = f.clone(), torch.zeros_like(f)
+        st = bp.pcg(lam, r, x, 1e-8, 3000, solver=nb.SOLVER_MIXED, precond=nb.PRECOND_LEARNED,
+                    net=net)
+        assert st["status"] == 0 and st["true_rel_res"] <= 1e-8
+        its[mode] = st["iterations"]
+    assert abs(its[nb.NET_TENSOR_TC5] - its[nb.NET_TENSOR_SYNC]) <= 0.1 * its[nb.NET_TENSOR_SYNC] + 5, its
 
 
 def test_inference_mode_falls_back_where_not_built(nb):
