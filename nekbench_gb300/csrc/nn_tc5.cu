@@ -205,6 +205,28 @@ __device__ __forceinline__ float block_sum4(float v, float* red)
   return red[0] + red[1] + red[2] + red[3];
 }
 
+// the MMAs of one layer, issued by one thread: tile t accumulates NMAT
+// products of K = 16 into TMEM columns NCOL * t onwards (A shifted by the tap's
+// (dj, dk) rows, B the tap's weight matrix), then commits to its barrier.
+// Fully unrolled: every descriptor is a base plus an immediate offset.
+template <int NMAT, int BSTRIDE, int NCOL, bool L1>
+__device__ __forceinline__ void issue_layer(uint32_t tmem, uint64_t da, uint64_t db, uint32_t id,
+                                            uint32_t bar_t)
+{
+  fence_after();
+#pragma unroll
+  for (int t = 0; t < kTiles; ++t) {
+#pragma unroll
+    for (int b = 0; b < NMAT; ++b) {
+      const int dj = L1 ? b - 1 : b % 3 - 1, dk = L1 ? 0 : b / 3 - 1;
+      const int grp = (kLead + kTile0 + 128 * t + 8 * dj + kPlaneRows * dk) / 8;  // 256-byte row groups
+      mma(tmem + (uint32_t)(NCOL * t), da + (uint64_t)(grp * 16), db + (uint64_t)(b * BSTRIDE / 16), id,
+          b > 0 ? 1u : 0u);
+    }
+    commit(bar_t + 8 * t);
+  }
+}
+
 // B operands, [n][k] K-major in core matrices: element (n, k) at
 // ((n/8)*2 + k/8)*128 + (n%8)*16 + (k%8)*2
 __device__ __forceinline__ int wb_off(int n, int k) { return ((n >> 3) * 2 + (k >> 3)) * 128 + (n & 7) * 16 + (k & 7) * 2; }
@@ -291,22 +313,10 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
   bool failed = false, input_failed = false, copy_pending = false;
   const int i = lane & 7;  // node i of this thread's rows (tile rows start at multiples of 8)
 
-  // issue the MMAs of one layer: tile t accumulates nmat K=16 products into
-  // TMEM columns ncol * t onwards, then commits to its barrier
-  auto issue = [&](uint32_t sA, uint32_t sB, int bstride, int nmat, int ncol, uint32_t id, bool l1) {
-    if (tid != 0) return;
-    fence_after();
-#pragma unroll 1
-    for (int t = 0; t < kTiles; ++t) {
-      for (int b = 0; b < nmat; ++b) {
-        const int dj = l1 ? b - 1 : b % 3 - 1, dk = l1 ? 0 : b / 3 - 1;
-        const int row0 = kLead + kTile0 + 128 * t + 8 * dj + kPlaneRows * dk;
-        mma(tmem + (uint32_t)(ncol * t), sdesc(sA + (uint32_t)(row0 / 8) * 256),
-            sdesc(sB + (uint32_t)(b * bstride)), id, b > 0 ? 1u : 0u);
-      }
-      commit(bar_t + 8 * t);
-    }
-  };
+  // shared-memory descriptors of the operand buffers; an offset of whole
+  // 16-byte units is added to the descriptor's start-address field
+  const uint64_t dX = sdesc(sX), dY = sdesc(sY);
+  const uint64_t dW1 = sdesc(sW1), dW2 = sdesc(sW2), dW3 = sdesc(sW3);
   auto wait_tile = [&](int t) -> bool {
     const bool ok = bar_wait(bar_t + 8 * t, tphase & 1u);
     fence_after();
@@ -374,7 +384,7 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
     __syncthreads();
 
     // ---- layer 1: 1 -> 16, GELU, into Y
-    issue(sX, sW1, 512, 3, 16, idesc_n(16), true);
+    if (tid == 0) issue_layer<3, 512, 16, true>(tmem, dX, dW1, idesc_n(16), bar_t);
     bool ok = true;
 #pragma unroll 1
     for (int t = 0; t < kTiles; ++t) {
@@ -395,7 +405,7 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
     if (__syncthreads_or(!ok)) { failed = true; break; }
 
     // ---- layer 2: 16 -> 16, GELU, into X
-    issue(sY, sW2, 1536, 9, 48, idesc_n(48), false);
+    if (tid == 0) issue_layer<9, 1536, 48, false>(tmem, dY, dW2, idesc_n(48), bar_t);
 #pragma unroll 1
     for (int t = 0; t < kTiles; ++t) {
       ok = wait_tile(t) && ok;
@@ -424,7 +434,7 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
     if (__syncthreads_or(!ok)) { failed = true; break; }
 
     // ---- layer 3: 16 -> 1 and the output
-    issue(sX, sW3, 512, 9, 16, idesc_n(16), false);
+    if (tid == 0) issue_layer<9, 512, 16, false>(tmem, dX, dW3, idesc_n(16), bar_t);
 #pragma unroll 1
     for (int t = 0; t < kTiles; ++t) {
       ok = wait_tile(t) && ok;
