@@ -434,7 +434,11 @@ int net_infer_tc(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const f
   NEKB_CUDA(cudaGetDevice(&dev));
   NEKB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   NEKB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_net_infer_tc, kThreads, kSmTotal));
-  int64_t grid = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
+  // two CTAs fit an SM by the launch bounds and the shared-memory plan; the
+  // occupancy query has reported one for such kernels
+  static_assert(2 * (kSmTotal + 1024) <= 233472, "two CTAs fit one SM's shared memory");
+  if (per_sm < 2) per_sm = 2;
+  int64_t grid = (int64_t)sms * per_sm;
   if (grid > Etot) grid = Etot;
   if (grid < 1) return NEKB_OK;
   k_net_infer_tc<<<(unsigned)grid, kThreads, kSmTotal, s>>>(Etot, Efield, Wbf, r, w, invDiag, out,

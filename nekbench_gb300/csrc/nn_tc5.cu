@@ -24,14 +24,17 @@
 // N = 16 (columns di = -1, 0, 1 used).  Every TMEM read-back stays in the
 // reading warp's own 32 lanes: no shared-memory round trip of the partial sums.
 //
-// One CTA of 4 warps per element at a time (persistent grid, two CTAs per SM,
-// 256 TMEM columns each: layer 2 holds 5 x 48).  Thread 0 issues the MMAs of a
+// One CTA of 4 warps per element at a time, three CTAs per SM (persistent
+// grid; 75 KB of shared memory and 128 TMEM columns each), so that each warp
+// scheduler has three warps to switch between.  Thread 0 issues the MMAs of a
 // layer tile by tile and commits each tile to its own mbarrier, so the
 // epilogue of tile t (TMEM -> registers, shuffles, GELU, BF16, next layer's
-// operand) overlaps the MMAs of the later tiles.  The next element's input
-// rows arrive by bulk asynchronous copies meanwhile.  Every wait is bounded;
-// a wait that runs out sets a device flag, the CTA waits (bounded) for its
-// operations in flight, frees its TMEM and returns.
+// operand) overlaps the MMAs of the later tiles.  Layer 2's accumulators
+// (5 tiles x 48 columns) cycle through two 48-column buffers: tile t + 2 is
+// issued once every warp has read tile t.  Inputs are read straight from
+// global memory.  Every wait is bounded; a wait that runs out sets a device
+// flag, the CTA waits (bounded) for its operations in flight, frees its TMEM
+// and returns.
 //
 // Arithmetic: BF16 weights and activations (the scaled input and both GELU
 // outputs rounded to BF16), FP32 accumulation, the tanh form of GELU with the
@@ -56,21 +59,21 @@ constexpr int kActBytes = kRows * 32;    // one activation buffer
 constexpr int kSmW1 = 0;                         // 3 x [16 n][16 k] bf16
 constexpr int kSmW2 = kSmW1 + 3 * 512;           // 9 x [48 n][16 k]
 constexpr int kSmW3 = kSmW2 + 9 * 1536;          // 9 x [16 n][16 k]
-constexpr int kSmX = 20480;                      // layer-1 im2col, then layer-2 output
-constexpr int kSmY = kSmX + kActBytes + 512;     // layer-1 output (47104)
-constexpr int kSmIn = kSmY + kActBytes;          // [2 buffers][r, invDiag, w][512] floats
-constexpr int kSmH = kSmIn + 2 * 3 * kNp * 4;    // sqrt(invDiag), 512 floats
+constexpr int kSmX = kSmW3 + 9 * 512;            // layer-1 im2col, then layer-2 output (19968)
+constexpr int kSmY = kSmX + kActBytes;           // layer-1 output
+constexpr int kSmH = kSmY + kActBytes;           // sqrt(invDiag), 512 floats
 constexpr int kSmA0 = kSmH + kNp * 4;            // scaled input (BF16 values), 512 floats
 constexpr int kSmRed = kSmA0 + kNp * 4;          // block sums
-constexpr int kSmBar = kSmRed + 64;              // 2 input + 5 tile mbarriers
-constexpr int kSmSlot = kSmBar + 8 * 8;          // TMEM base address
+constexpr int kSmBar = kSmRed + 64;              // 5 tile mbarriers
+constexpr int kSmSlot = kSmBar + kTiles * 8;     // TMEM base address
 constexpr int kSmTotal = kSmSlot + 16;
-constexpr int kRowBytes = kNp * 4;
-constexpr uint32_t kTmemCols = 256;
+constexpr int kCtasPerSm = 3;
+constexpr uint32_t kTmemCols = 128;              // layers 1 and 3: 5 x 16; layer 2: 2 x 48
 constexpr long kWaitLimit = 1L << 22;
 
-static_assert(kSmX % 1024 == 0 && kSmY % 256 == 0, "operand buffers aligned");
-static_assert(kSmTotal * 3 > 227 * 1024, "at most two CTAs per SM share the 512 TMEM columns");
+static_assert(kSmX % 256 == 0 && kSmY % 256 == 0, "operand buffers aligned");
+static_assert(kCtasPerSm * (kSmTotal + 1024) <= 233472, "three CTAs fit one SM's shared memory");
+static_assert(kCtasPerSm * kTmemCols <= 512, "the resident CTAs share the 512 TMEM columns");
 
 // set when a wait (input copy or MMA) did not complete within kWaitLimit polls
 __device__ int g_tc5_timeout;
@@ -165,19 +168,6 @@ __device__ __forceinline__ void bar_init(uint32_t bar)
   asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
 }
 
-__device__ __forceinline__ void bar_expect(uint32_t bar, uint32_t bytes)
-{
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ void bulk_row(uint32_t dst, const float* src, uint32_t bar)
-{
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
-      "l"(src), "r"((uint32_t)kRowBytes), "r"(bar)
-      : "memory");
-}
-
 // true once the barrier has completed the phase with the given parity; false
 // after kWaitLimit polls
 __device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity)
@@ -205,23 +195,25 @@ __device__ __forceinline__ float block_sum4(float v, float* red)
   return red[0] + red[1] + red[2] + red[3];
 }
 
-// the MMAs of one layer, issued by one thread: tile t accumulates NMAT
-// products of K = 16 into TMEM columns NCOL * t onwards (A shifted by the tap's
-// (dj, dk) rows, B the tap's weight matrix), then commits to its barrier.
-// Fully unrolled: every descriptor is a base plus an immediate offset.
+// MMAs of tiles t0 .. t1-1 of one layer, issued by one thread: tile t
+// accumulates NMAT products of K = 16 into TMEM columns NCOL * (t % RING)
+// (RING = 0: NCOL * t) onwards -- A shifted by the tap's (dj, dk) rows, B the
+// tap's weight matrix -- then commits to its barrier.  Fully unrolled over the
+// taps: every descriptor is a base plus an immediate offset.
 template <int NMAT, int BSTRIDE, int NCOL, bool L1>
-__device__ __forceinline__ void issue_layer(uint32_t tmem, uint64_t da, uint64_t db, uint32_t id,
-                                            uint32_t bar_t)
+__device__ __forceinline__ void issue_tiles(uint32_t tmem, uint64_t da, uint64_t db, uint32_t id,
+                                            uint32_t bar_t, int t0, int t1, int ring)
 {
   fence_after();
-#pragma unroll
-  for (int t = 0; t < kTiles; ++t) {
+#pragma unroll 1
+  for (int t = t0; t < t1; ++t) {
+    const uint32_t d = tmem + (uint32_t)(NCOL * (ring ? t % ring : t));
+    const uint64_t at = da + (uint64_t)(t * 128 * 16 / 8);  // 128 rows = 16 row groups of 16 units
 #pragma unroll
     for (int b = 0; b < NMAT; ++b) {
       const int dj = L1 ? b - 1 : b % 3 - 1, dk = L1 ? 0 : b / 3 - 1;
-      const int grp = (kLead + kTile0 + 128 * t + 8 * dj + kPlaneRows * dk) / 8;  // 256-byte row groups
-      mma(tmem + (uint32_t)(NCOL * t), da + (uint64_t)(grp * 16), db + (uint64_t)(b * BSTRIDE / 16), id,
-          b > 0 ? 1u : 0u);
+      const int grp = (kLead + kTile0 + 8 * dj + kPlaneRows * dk) / 8;  // 256-byte row groups
+      mma(d, at + (uint64_t)(grp * 16), db + (uint64_t)(b * BSTRIDE / 16), id, b > 0 ? 1u : 0u);
     }
     commit(bar_t + 8 * t);
   }
@@ -231,7 +223,7 @@ __device__ __forceinline__ void issue_layer(uint32_t tmem, uint64_t da, uint64_t
 // ((n/8)*2 + k/8)*128 + (n%8)*16 + (k%8)*2
 __device__ __forceinline__ int wb_off(int n, int k) { return ((n >> 3) * 2 + (k >> 3)) * 128 + (n & 7) * 16 + (k & 7) * 2; }
 
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, kCtasPerSm)
 k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ Wbf,
                 const float* __restrict__ r, const float* __restrict__ w, const float* __restrict__ invDiag,
                 float* __restrict__ out, int normalize, const int* skip)
@@ -245,9 +237,7 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
   float* red = reinterpret_cast<float*>(smem + kSmRed);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint16_t* W = reinterpret_cast<const uint16_t*>(Wbf);
-  const uint32_t bar_in = smem_addr(smem + kSmBar), bar_t = bar_in + 16;
-  const uint32_t sW1 = smem_addr(smem + kSmW1), sW2 = smem_addr(smem + kSmW2), sW3 = smem_addr(smem + kSmW3);
-  const uint32_t sX = smem_addr(X), sY = smem_addr(Y);
+  const uint32_t bar_t = smem_addr(smem + kSmBar);
 
   // ---- weights as B operands (once per CTA); both activation buffers zeroed
   // (their padding rows are never written again)
@@ -278,7 +268,7 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
     reinterpret_cast<uint4*>(Y)[x] = make_uint4(0, 0, 0, 0);
   }
   if (tid == 0) {
-    for (int b = 0; b < 2 + kTiles; ++b) bar_init(bar_in + 8 * b);
+    for (int b = 0; b < kTiles; ++b) bar_init(bar_t + 8 * b);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   fence_async_smem();
@@ -295,54 +285,31 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
   const uint32_t tmem = *slot;
   const uint32_t tlane = tmem + ((uint32_t)(32 * warp) << 16);  // this warp's TMEM lanes
 
-  // input rows r, invDiag, w of an element, double-buffered, by bulk copies
-  const float* inb = reinterpret_cast<const float*>(smem + kSmIn);
-  const uint32_t in_s = smem_addr(smem + kSmIn);
-  const uint32_t nrows = 1u + (invDiag ? 1u : 0u) + (w ? 1u : 0u);
-  auto fetch = [&](int64_t el, int buf) {
-    const uint32_t bar = bar_in + 8 * buf, dst = in_s + buf * 3 * kRowBytes;
-    bar_expect(bar, nrows * kRowBytes);
-    bulk_row(dst, r + el * kNp, bar);
-    if (invDiag) bulk_row(dst + kRowBytes, invDiag + (el % Efield) * kNp, bar);
-    if (w) bulk_row(dst + 2 * kRowBytes, w + (el % Efield) * kNp, bar);
-  };
-  if (tid == 0 && (int64_t)blockIdx.x < Etot) fetch(blockIdx.x, 0);
-  uint32_t pin[2] = {0u, 0u};
-  uint32_t tphase = 0;  // completed phases of every tile barrier
-  int buf = 0;
-  bool failed = false, input_failed = false, copy_pending = false;
-  const int i = lane & 7;  // node i of this thread's rows (tile rows start at multiples of 8)
-
   // shared-memory descriptors of the operand buffers; an offset of whole
   // 16-byte units is added to the descriptor's start-address field
-  const uint64_t dX = sdesc(sX), dY = sdesc(sY);
-  const uint64_t dW1 = sdesc(sW1), dW2 = sdesc(sW2), dW3 = sdesc(sW3);
+  const uint64_t dX = sdesc(smem_addr(X)), dY = sdesc(smem_addr(Y));
+  const uint64_t dW1 = sdesc(smem_addr(smem + kSmW1)), dW2 = sdesc(smem_addr(smem + kSmW2));
+  const uint64_t dW3 = sdesc(smem_addr(smem + kSmW3));
+  uint32_t tphase = 0;  // completed phases of every tile barrier
+  bool failed = false;
+  const int i = lane & 7;  // node i of this thread's rows (tile rows start at multiples of 8)
   auto wait_tile = [&](int t) -> bool {
     const bool ok = bar_wait(bar_t + 8 * t, tphase & 1u);
     fence_after();
     return ok;
   };
 
-  for (int64_t e = blockIdx.x; e < Etot; e += gridDim.x, buf ^= 1) {
-    const bool next = e + gridDim.x < Etot;
-    if (tid == 0 && next) {
-      fence_async_smem();  // the other buffer's reads are done
-      fetch(e + gridDim.x, buf ^ 1);
-    }
-    copy_pending = next;
-    const bool okin = bar_wait(bar_in + 8 * buf, pin[buf]);
-    pin[buf] ^= 1u;
-    if (__syncthreads_or(!okin)) { failed = true; input_failed = true; break; }
-    const float* rin = inb + buf * 3 * kNp;
-    const float* din = rin + kNp;
-    const float* win = rin + 2 * kNp;
+  for (int64_t e = blockIdx.x; e < Etot; e += gridDim.x) {
+    const float* rin = r + e * kNp;
+    const float* din = invDiag ? invDiag + (e % Efield) * kNp : nullptr;
+    const float* win = w ? w + (e % Efield) * kNp : nullptr;
 
     // ---- scaled input a0 = bf16(h r / s)
     float ss = 0.f;
 #pragma unroll
     for (int c = 0; c < kNp / kThreads; ++c) {
       const int n = tid + c * kThreads;
-      const float h = invDiag ? sqrtf(din[n]) : 1.f;
+      const float h = din ? sqrtf(din[n]) : 1.f;
       const float v = h * rin[n];
       hs[n] = h;
       a0[n] = v;
@@ -383,8 +350,8 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
     fence_before();
     __syncthreads();
 
-    // ---- layer 1: 1 -> 16, GELU, into Y
-    if (tid == 0) issue_layer<3, 512, 16, true>(tmem, dX, dW1, idesc_n(16), bar_t);
+    // ---- layer 1: 1 -> 16, GELU, into Y (TMEM columns 16 t)
+    if (tid == 0) issue_tiles<3, 512, 16, true>(tmem, dX, dW1, idesc_n(16), bar_t, 0, kTiles, 0);
     bool ok = true;
 #pragma unroll 1
     for (int t = 0; t < kTiles; ++t) {
@@ -404,16 +371,23 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
     fence_before();
     if (__syncthreads_or(!ok)) { failed = true; break; }
 
-    // ---- layer 2: 16 -> 16, GELU, into X
-    if (tid == 0) issue_layer<9, 1536, 48, false>(tmem, dY, dW2, idesc_n(48), bar_t);
+    // ---- layer 2: 16 -> 16, GELU, into X; accumulators in two 48-column
+    // buffers (tile t in columns 48 (t % 2))
+    if (tid == 0) issue_tiles<9, 1536, 48, false>(tmem, dY, dW2, idesc_n(48), bar_t, 0, 2, 2);
 #pragma unroll 1
     for (int t = 0; t < kTiles; ++t) {
       ok = wait_tile(t) && ok;
       float vm[16], v0[16], vp[16];
-      ld16(tlane + (uint32_t)(48 * t), vm);
-      ld16(tlane + (uint32_t)(48 * t + 16), v0);
-      ld16(tlane + (uint32_t)(48 * t + 32), vp);
+      const uint32_t col = (uint32_t)(48 * (t & 1));
+      ld16(tlane + col, vm);
+      ld16(tlane + col + 16, v0);
+      ld16(tlane + col + 32, vp);
       ld_wait();
+      if (t + 2 < kTiles) {  // every warp has read buffer t % 2: reuse it for tile t + 2
+        fence_before();
+        __syncthreads();
+        if (tid == 0) issue_tiles<9, 1536, 48, false>(tmem, dY, dW2, idesc_n(48), bar_t, t + 2, t + 3, 2);
+      }
       const int np = kTile0 + 128 * t + 32 * warp + lane;
       const int jp = (np >> 3) % 10;
       const bool live = jp >= 1 && jp <= kNq;
@@ -433,8 +407,8 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
     fence_before();
     if (__syncthreads_or(!ok)) { failed = true; break; }
 
-    // ---- layer 3: 16 -> 1 and the output
-    if (tid == 0) issue_layer<9, 512, 16, false>(tmem, dX, dW3, idesc_n(16), bar_t);
+    // ---- layer 3: 16 -> 1 and the output (TMEM columns 16 t)
+    if (tid == 0) issue_tiles<9, 512, 16, false>(tmem, dX, dW3, idesc_n(16), bar_t, 0, kTiles, 0);
 #pragma unroll 1
     for (int t = 0; t < kTiles; ++t) {
       ok = wait_tile(t) && ok;
@@ -451,8 +425,8 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
       if (jp >= 1 && jp <= kNq) {
         const int n = i + kNq * (jp - 1) + kNq * kNq * (kp - 1);
         o *= hs[n] * s;
-        if ((normalize & kNetAddJacobi) && invDiag) o += din[n] * rin[n];
-        out[e * kNp + n] = (w ? win[n] : 1.f) * o;
+        if ((normalize & kNetAddJacobi) && din) o += din[n] * rin[n];
+        out[e * kNp + n] = (win ? win[n] : 1.f) * o;
       }
     }
     ++tphase;
@@ -460,15 +434,10 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
     if (__syncthreads_or(!ok)) { failed = true; break; }
   }
 
-  if (failed) {  // flag, then wait (bounded) for this CTA's operations in flight
+  if (failed) {  // flag, then wait (bounded) for this CTA's MMAs in flight
     if (tid == 0) {
       atomicExch(&g_tc5_timeout, 1);
-      if (input_failed) {
-        bar_wait(bar_in + 8 * buf, pin[buf] ^ 1u);  // the copy that did not arrive
-      } else {
-        for (int t = 0; t < kTiles; ++t) bar_wait(bar_t + 8 * t, tphase & 1u);
-      }
-      if (copy_pending) bar_wait(bar_in + 8 * (buf ^ 1), pin[buf ^ 1]);
+      for (int t = 0; t < kTiles; ++t) bar_wait(bar_t + 8 * t, tphase & 1u);
     }
     fence_before();
     __syncthreads();
@@ -501,18 +470,15 @@ int net_tc5_raise_timeout()
 int net_infer_tc5(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const float* r, const float* w,
                   const float* invDiag, float* out, int normalize, const int* skip, cudaStream_t s)
 {
-  for (const void* p : {(const void*)r, (const void*)w, (const void*)invDiag})
-    if (reinterpret_cast<uintptr_t>(p) % 16 != 0)
-      return fail(NEKB_ERR_INVALID, "network: input arrays must be 16-byte aligned");
   static SmemOptIn smem_opt;
   NEKB_TRY(smem_opt.ensure(k_net_infer_tc5, kSmTotal));
-  int dev = 0, sms = 152, per_sm = 0;
+  int dev = 0, sms = 152;
   NEKB_CUDA(cudaGetDevice(&dev));
   NEKB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  NEKB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_net_infer_tc5, kThreads, kSmTotal));
-  if (per_sm < 1) per_sm = 1;
-  if (per_sm > 2) per_sm = 2;  // 2 x 256 TMEM columns per SM
-  int64_t grid = (int64_t)sms * per_sm;
+  // kCtasPerSm CTAs fit an SM by construction (the static_asserts above); the
+  // occupancy query is not used, as it reported one CTA per SM for a kernel
+  // of which two fit
+  int64_t grid = (int64_t)sms * kCtasPerSm;
   if (grid > Etot) grid = Etot;
   if (grid < 1) return NEKB_OK;
   k_net_infer_tc5<<<(unsigned)grid, kThreads, kSmTotal, s>>>(Etot, Efield, Wbf, r, w, invDiag, out,
