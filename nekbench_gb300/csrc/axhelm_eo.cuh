@@ -51,12 +51,7 @@ struct CfgEO {
   static constexpr int HP = H + ODD;       // pair tasks per line (incl. the middle line)
   static constexpr int NQ2 = NQ * NQ;
   static constexpr int NP = NQ2 * NQ;
-  // shared node arrays: row stride NQ + 1 and plane stride NQ (NQ + 1) + 2, so
-  // that the lines a warp reads together fall into distinct banks
-  static constexpr int RS = NQ + 1;
-  static constexpr int PS = NQ * RS + 2;
-  static constexpr int SNP = NQ * PS;
-  static constexpr int PER_EL = 4 * SNP * 8;  // four node arrays per element, fields in turn
+  static constexpr int PER_EL = 4 * NP * 8;  // four node arrays per element, fields in turn
   static constexpr int CAP = 100 * 1024;     // two CTAs per SM
   static constexpr int nel_fit(int n) { return (n <= 1 || n * PER_EL <= CAP) ? n : nel_fit(n - 1); }
   static constexpr int NEL0 = (256 / NQ2) > 0 ? (256 / NQ2) : 1;
@@ -67,7 +62,7 @@ struct CfgEO {
   // per matrix (D, then D^T): P[HP][H] (s rows; row H = middle row, NQ odd)
   // and M[HP][HM] (d rows; row H is zero)
   static constexpr int TAB = HP * H + HP * HM;
-  static constexpr int SMEM = (DPAD + 2 * TAB + NEL * 4 * SNP) * 8;
+  static constexpr int SMEM = (DPAD + 2 * TAB + NEL * 4 * NP) * 8;
 };
 
 #ifndef EO_L2_PREFETCH
@@ -150,17 +145,17 @@ __device__ __forceinline__ void pair_tasks(const double* T, double* Q, int a, in
                                            const double* P, const double* M)
 {
   using C = CfgEO<NQ>;
-  constexpr int H = C::H, HM = C::HM, HP = C::HP, RS = C::RS, PS = C::PS;
-  constexpr int stride = RDIR ? 1 : RS;
-  const int cross = RDIR ? b * RS : b;  // offset of the line inside its plane
+  constexpr int H = C::H, HM = C::HM, HP = C::HP, NQ2 = C::NQ2;
+  constexpr int stride = RDIR ? 1 : NQ;
+  const int cross = RDIR ? b * NQ : b;  // offset of the line inside its plane
 #pragma unroll
   for (int t = 0; t < HP; ++t) {
     const int tau = a * HP + t;  // (pair, plane) task index of this line
     const int p = tau / NQ, k = tau - p * NQ;
-    const double* line = T + k * PS + cross;
+    const double* line = T + k * NQ2 + cross;
     double s, d;
     pair_sd<NQ>(line, stride, P + p * H, M + p * HM, s, d);
-    double* out = Q + k * PS + cross;
+    double* out = Q + k * NQ2 + cross;
     out[p * stride] = s + d;
     out[(NQ - 1 - p) * stride] = s - d;  // the same node and value for the middle line
   }
@@ -174,8 +169,7 @@ __device__ __forceinline__ void direct_field(const AxArgs& a, int f, int64_t ele
                                              double* A0, double* A1, double* A2, double& qaq)
 {
   using C = CfgEO<NQ>;
-  constexpr int NQ2 = C::NQ2, NP = C::NP, DS = C::DS, RS = C::RS, PS = C::PS;
-  const int sij = j * RS + i;  // the thread's column in the shared arrays
+  constexpr int NQ2 = C::NQ2, NP = C::NP, DS = C::DS;
   const double* ge = static_cast<const double*>(a.ggeo) + element * 7 * NP + ij;
   const double* lam = static_cast<const double*>(a.lambda);
   double r_q[NQ], r_Gt[NQ];
@@ -184,19 +178,19 @@ __device__ __forceinline__ void direct_field(const AxArgs& a, int f, int64_t ele
 #pragma unroll
     for (int k = 0; k < NQ; ++k) {
       r_q[k] = qe[k * NQ2];
-      A0[k * PS + sij] = r_q[k];
+      A0[k * NQ2 + ij] = r_q[k];
     }
   }
   __syncthreads();
   if (active) {
 #pragma unroll
     for (int k = 0; k < NQ; ++k) {
-      const int n = k * PS + sij;
+      const int n = k * NQ2 + ij;
       double qr = 0, qs = 0, qt = 0;
 #pragma unroll
       for (int m = 0; m < NQ; ++m) {
-        qr += s_D[i * DS + m] * A0[k * PS + j * RS + m];
-        qs += s_D[j * DS + m] * A0[k * PS + m * RS + i];
+        qr += s_D[i * DS + m] * A0[k * NQ2 + j * NQ + m];
+        qs += s_D[j * DS + m] * A0[k * NQ2 + m * NQ + i];
         qt += s_D[k * DS + m] * r_q[m];
       }
       const double G00 = ge[1 * NP + k * NQ2], G01 = ge[2 * NP + k * NQ2];
@@ -206,7 +200,7 @@ __device__ __forceinline__ void direct_field(const AxArgs& a, int f, int64_t ele
       double gs = G01 * qr + G11 * qs + G12 * qt;
       double gt = G02 * qr + G12 * qs + G22 * qt;
       if (!BK) {
-        const double lam0 = lam[element * NP + k * NQ2 + ij];
+        const double lam0 = lam[element * NP + n];
         gr *= lam0;
         gs *= lam0;
         gt *= lam0;
@@ -224,8 +218,8 @@ __device__ __forceinline__ void direct_field(const AxArgs& a, int f, int64_t ele
       double ar = 0, as = 0, at = 0;
 #pragma unroll
       for (int m = 0; m < NQ; ++m) {
-        ar += s_D[m * DS + i] * A1[k * PS + j * RS + m];
-        as += s_D[m * DS + j] * A2[k * PS + m * RS + i];
+        ar += s_D[m * DS + i] * A1[k * NQ2 + j * NQ + m];
+        as += s_D[m * DS + j] * A2[k * NQ2 + m * NQ + i];
         at += s_D[m * DS + k] * r_Gt[m];
       }
       double out = ar + as + at;
@@ -246,7 +240,7 @@ __global__ void __launch_bounds__(CfgEO<NQ>::THREADS, EO_MIN_BLOCKS) k_axhelm_eo
 {
   using C = CfgEO<NQ>;
   constexpr int H = C::H, HM = C::HM, HP = C::HP, NQ2 = C::NQ2, NP = C::NP, NEL = C::NEL;
-  constexpr int DS = C::DS, RS = C::RS, PS = C::PS, SNP = C::SNP;
+  constexpr int DS = C::DS;
   if (a.skip != nullptr && *a.skip != 0) return;
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -307,16 +301,15 @@ __global__ void __launch_bounds__(CfgEO<NQ>::THREADS, EO_MIN_BLOCKS) k_axhelm_eo
   const int i = ij % NQ;
   const int j = ij / NQ;
   const int ip = NQ - 1 - i, jp = NQ - 1 - j;
-  const int sij = j * RS + i;  // the thread's column in the shared arrays
   const int64_t eidx = (int64_t)blockIdx.x * NEL + el;
   const bool active = (el < NEL) && (eidx < a.Nelements);
   int64_t element = eidx;
   if (PARTIAL && active) element = a.elementList[eidx];
   const int elc = active ? el : 0;  // keep shared pointers in range for idle threads
-  double* A0 = s_all + elc * 4 * SNP;
-  double* A1 = A0 + SNP;
-  double* A2 = A1 + SNP;
-  double* A3 = A2 + SNP;
+  double* A0 = s_all + elc * 4 * NP;
+  double* A1 = A0 + NP;
+  double* A2 = A1 + NP;
+  double* A3 = A2 + NP;
 
   const double* ge = static_cast<const double*>(a.ggeo) + element * 7 * NP + ij;
   const double* lam = static_cast<const double*>(a.lambda);
@@ -349,8 +342,8 @@ __global__ void __launch_bounds__(CfgEO<NQ>::THREADS, EO_MIN_BLOCKS) k_axhelm_eo
         const double vi = qe[k * NQ2 + (ip - i)];
         const double vj = qe[k * NQ2 + (jp - j) * NQ];
         r_q[k] = v;
-        A0[k * PS + sij] = eo_value(v, vi, i, ip);
-        A1[k * PS + sij] = eo_value(v, vj, j, jp);
+        A0[k * NQ2 + ij] = eo_value(v, vi, i, ip);
+        A1[k * NQ2 + ij] = eo_value(v, vj, j, jp);
       }
       line_eo<NQ>(r_q, qt, s_P1, s_M1);  // t direction
     }
@@ -364,7 +357,7 @@ __global__ void __launch_bounds__(CfgEO<NQ>::THREADS, EO_MIN_BLOCKS) k_axhelm_eo
     if (active) {
 #pragma unroll
       for (int k = 0; k < NQ; ++k) {
-        const int n = k * PS + sij;
+        const int n = k * NQ2 + ij;
         const double qr = A2[n], qs = A3[n];
         const double G00 = ge[1 * NP + k * NQ2], G01 = ge[2 * NP + k * NQ2];
         const double G02 = ge[3 * NP + k * NQ2], G11 = ge[4 * NP + k * NQ2];
@@ -373,7 +366,7 @@ __global__ void __launch_bounds__(CfgEO<NQ>::THREADS, EO_MIN_BLOCKS) k_axhelm_eo
         double gs = G01 * qr + G11 * qs + G12 * qt[k];
         double g3 = G02 * qr + G12 * qs + G22 * qt[k];
         if (!BK) {
-          const double lam0 = lam[element * NP + k * NQ2 + ij];
+          const double lam0 = lam[element * NP + n];
           gr *= lam0;
           gs *= lam0;
           g3 *= lam0;
@@ -388,9 +381,9 @@ __global__ void __launch_bounds__(CfgEO<NQ>::THREADS, EO_MIN_BLOCKS) k_axhelm_eo
     if (active) {
 #pragma unroll
       for (int k = 0; k < NQ; ++k) {
-        const int n = k * PS + sij;
+        const int n = k * NQ2 + ij;
         A2[n] = eo_value(A0[n], A0[n + (ip - i)], i, ip);
-        A3[n] = eo_value(A1[n], A1[n + (jp - j) * RS], j, jp);
+        A3[n] = eo_value(A1[n], A1[n + (jp - j) * NQ], j, jp);
       }
       line_eo<NQ>(gt, at, s_P2, s_M2);  // t direction, D^T
     }
@@ -404,9 +397,9 @@ __global__ void __launch_bounds__(CfgEO<NQ>::THREADS, EO_MIN_BLOCKS) k_axhelm_eo
       double* Aqe = static_cast<double*>(a.Aq) + f * a.offset + element * NP + ij;
 #pragma unroll
       for (int k = 0; k < NQ; ++k) {
-        const int n = k * PS + sij;
+        const int n = k * NQ2 + ij;
         double out = A0[n] + A1[n] + at[k];
-        if (!BK) out += (ge[k * NQ2] * lam[element * NP + k * NQ2 + ij + a.offset]) * r_q[k];
+        if (!BK) out += (ge[k * NQ2] * lam[element * NP + n + a.offset]) * r_q[k];
         Aqe[k * NQ2] = out;
         qaq += r_q[k] * out;
       }

@@ -590,7 +590,7 @@ int run_train(nekb_net* net, int64_t E, const float* in, const float* target, cu
   return fail(NEKB_ERR_UNSUPPORTED, "net: Nq=%d C=%d not built (Nq 4/6/8, C 4/8/16)", net->Nq, net->C);
 
 // the tensor-core kernel NEKB_NET_TENSOR selects
-constexpr int kTensorDefault = NEKB_NET_TENSOR_SYNC;
+constexpr int kTensorDefault = NEKB_NET_TENSOR_TC5;
 
 int net_infer(const nekb_net* net, int64_t Etot, int64_t Efield, const float* r, const float* w,
               const float* invDiag, float* out, int normalize, const int* skip, cudaStream_t s)

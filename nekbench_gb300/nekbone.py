@@ -40,6 +40,9 @@ def parse(argv=None):
     p.add_argument("--precond", default=None, choices=("jacobi", "copy", "learned"))
     p.add_argument("--weights", default=os.path.join(os.path.dirname(os.path.abspath(__file__)),
                                                       "weights", "precond_n7_c16.bin"))
+    p.add_argument("--inference", default="tensor", choices=("tensor", "tc5", "sync", "fp32"),
+                   help="network arithmetic: the default tensor-core kernel, tcgen05, mma.sync "
+                        "or FP32 cores")
     p.add_argument("--tol", type=float, default=1e-8)
     p.add_argument("--maxit", type=int, default=1000)
     p.add_argument("--fixed", action="store_true", help="FIXED ITERATION COUNT: exactly maxit")
@@ -99,6 +102,8 @@ def main(argv=None):
                                "fp32_trilinear": nb.FP32_TRILINEAR}[a.inner])
     if precond == "learned":
         kw["net"] = nb.Net.load(a.weights)
+        kw["net"].inference = {"tensor": nb.NET_TENSOR, "tc5": nb.NET_TENSOR_TC5,
+                               "sync": nb.NET_TENSOR_SYNC, "fp32": nb.NET_FP32}[a.inference]
         kw["solver"] = nb.SOLVER_MIXED
     lam_arg = None if a.bp_mode else lam
 
