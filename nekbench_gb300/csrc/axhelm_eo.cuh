@@ -65,19 +65,6 @@ struct CfgEO {
   static constexpr int SMEM = (DPAD + 2 * TAB + NEL * 4 * NP) * 8;
 };
 
-#ifndef EO_L2_PREFETCH
-#define EO_L2_PREFETCH 1
-#endif
-
-// bulk prefetch into L2 of the 16-byte-aligned part of [p, p + bytes)
-__device__ __forceinline__ void prefetch_l2(const char* p, int64_t bytes)
-{
-  const uintptr_t b = (reinterpret_cast<uintptr_t>(p) + 15) & ~uintptr_t(15);
-  const uintptr_t e = (reinterpret_cast<uintptr_t>(p) + bytes) & ~uintptr_t(15);
-  if (e > b)
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(b), "r"((uint32_t)(e - b)) : "memory");
-}
-
 // transformed value of node `pos` of a line from its own value and its
 // partner's (pos' = NQ-1-pos): e at pos < pos', o at pos > pos', the value
 // itself in the middle; one FP64 operation for every thread
@@ -231,12 +218,8 @@ __device__ __forceinline__ void direct_field(const AxArgs& a, int f, int64_t ele
   __syncthreads();  // the next field overwrites A0..A2
 }
 
-#ifndef EO_MIN_BLOCKS
-#define EO_MIN_BLOCKS 2
-#endif
-
 template <int NQ, int NF, bool BK, bool PARTIAL>
-__global__ void __launch_bounds__(CfgEO<NQ>::THREADS, EO_MIN_BLOCKS) k_axhelm_eo(const AxArgs a)
+__global__ void __launch_bounds__(CfgEO<NQ>::THREADS, 2) k_axhelm_eo(const AxArgs a)
 {
   using C = CfgEO<NQ>;
   constexpr int H = C::H, HM = C::HM, HP = C::HP, NQ2 = C::NQ2, NP = C::NP, NEL = C::NEL;
@@ -314,17 +297,6 @@ __global__ void __launch_bounds__(CfgEO<NQ>::THREADS, EO_MIN_BLOCKS) k_axhelm_eo
   const double* ge = static_cast<const double*>(a.ggeo) + element * 7 * NP + ij;
   const double* lam = static_cast<const double*>(a.lambda);
   double qaq = 0.0;  // this thread's share of q . Aq (when asked for)
-  // The geometric factors are first read after two barriers, by every warp at
-  // once; fetch the element's slots into L2 now so that those reads wait on L2
-  // rather than HBM.  The range is rounded inward to 16-byte boundaries, so it
-  // never leaves the element's arrays.
-  if (EO_L2_PREFETCH && active && ij == 0) {
-    prefetch_l2(reinterpret_cast<const char*>(ge + (BK ? NP : 0)), (BK ? 6 : 7) * NP * 8);
-    if (!BK) {
-      prefetch_l2(reinterpret_cast<const char*>(lam + element * NP), NP * 8);
-      prefetch_l2(reinterpret_cast<const char*>(lam + element * NP + a.offset), NP * 8);
-    }
-  }
 
 #pragma unroll 1
   for (int f = 0; f < NF; ++f) {
