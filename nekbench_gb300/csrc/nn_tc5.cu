@@ -38,10 +38,13 @@
 //
 // Arithmetic: BF16 weights and activations (the scaled input and both GELU
 // outputs rounded to BF16), FP32 accumulation, the tanh form of GELU with the
-// hardware tanh.  No counterpart in the reference.
+// hardware tanh, evaluated on packed pairs in half precision (its 11-bit
+// significands add less error than the BF16 rounding that follows).  No
+// counterpart in the reference.
 #include "nn.h"
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 namespace nekb {
 namespace {
@@ -139,12 +142,30 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi)
   return *reinterpret_cast<const uint32_t*>(&v);
 }
 
-__device__ __forceinline__ float gelu_tc(float x)
+// GELU (tanh form, as gelu_tc) of two values in packed half precision, the
+// result rounded to BF16: x (1 + 0.044715 x^2) keeps the cube from
+// overflowing before tanh saturates, and the half-precision steps (11-bit
+// significands) add less error than the BF16 rounding of the result.  Inputs
+// must be below 65504 in magnitude.
+__device__ __forceinline__ uint32_t gelu2_bf16(float a, float b)
 {
-  const float u = 0.7978845608028654f * (x + 0.044715f * x * x * x);
-  float t;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
-  return 0.5f * x * (1.0f + t);
+  const __half2 x = __floats2half2_rn(a, b);
+  const __half2 one = __float2half2_rn(1.0f), c1 = __float2half2_rn(0.044715f);
+  const __half2 c2 = __float2half2_rn(0.7978845608028654f), hf = __float2half2_rn(0.5f);
+  const __half2 t = __hfma2(c1, __hmul2(x, x), one);
+  const __half2 u = __hmul2(__hmul2(x, t), c2);
+  __half2 th;
+  asm("tanh.approx.f16x2 %0, %1;" : "=r"(*reinterpret_cast<uint32_t*>(&th)) : "r"(*reinterpret_cast<const uint32_t*>(&u)));
+  const __half2 hx = __hmul2(hf, x);
+  const float2 g = __half22float2(__hfma2(hx, th, hx));
+  return pack2(g.x, g.y);
+}
+
+// 16 channels (8 packed BF16 pairs) of one row into an operand buffer
+__device__ __forceinline__ void store_row_packed(unsigned char* buf, int row, const uint32_t (&p)[8])
+{
+  *reinterpret_cast<uint4*>(buf + core_off(row, 0)) = make_uint4(p[0], p[1], p[2], p[3]);
+  *reinterpret_cast<uint4*>(buf + core_off(row, 1)) = make_uint4(p[4], p[5], p[6], p[7]);
 }
 
 // 16 channels of one row into an operand buffer (two 16-byte stores)
@@ -299,6 +320,19 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
     return ok;
   };
 
+  // this thread's residual and diagonal values of the element it starts next,
+  // loaded one element ahead (nodes tid + 128 c)
+  float nr[kNp / kThreads], nd[kNp / kThreads];
+  auto load_inputs = [&](int64_t el) {
+#pragma unroll
+    for (int c = 0; c < kNp / kThreads; ++c) {
+      const int n = tid + c * kThreads;
+      nr[c] = el < Etot ? r[el * kNp + n] : 0.f;
+      nd[c] = (el < Etot && invDiag) ? invDiag[(el % Efield) * kNp + n] : 1.f;
+    }
+  };
+  load_inputs(blockIdx.x);
+
   for (int64_t e = blockIdx.x; e < Etot; e += gridDim.x) {
     const float* rin = r + e * kNp;
     const float* din = invDiag ? invDiag + (e % Efield) * kNp : nullptr;
@@ -309,8 +343,8 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
 #pragma unroll
     for (int c = 0; c < kNp / kThreads; ++c) {
       const int n = tid + c * kThreads;
-      const float h = din ? sqrtf(din[n]) : 1.f;
-      const float v = h * rin[n];
+      const float h = din ? sqrtf(nd[c]) : 1.f;
+      const float v = h * nr[c];
       hs[n] = h;
       a0[n] = v;
       ss += v * v;
@@ -362,9 +396,10 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
       const int np = kTile0 + 128 * t + 32 * warp + lane;
       const int jp = (np >> 3) % 10;
       const bool live = jp >= 1 && jp <= kNq;
+      uint32_t g[8];
 #pragma unroll
-      for (int c = 0; c < 16; ++c) v[c] = live ? gelu_tc(v[c]) : 0.f;
-      store_row(Y, np + kLead, v);
+      for (int c = 0; c < 8; ++c) g[c] = live ? gelu2_bf16(v[2 * c], v[2 * c + 1]) : 0u;
+      store_row_packed(Y, np + kLead, g);
     }
     ++tphase;
     fence_async_smem();
@@ -398,9 +433,12 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
         float o = v0[c];
         if (i < kNq - 1) o += up;
         if (i > 0) o += dn;
-        v0[c] = live ? gelu_tc(o) : 0.f;
+        v0[c] = o;
       }
-      store_row(X, np + kLead, v0);
+      uint32_t g[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) g[c] = live ? gelu2_bf16(v0[2 * c], v0[2 * c + 1]) : 0u;
+      store_row_packed(X, np + kLead, g);
     }
     ++tphase;
     fence_async_smem();
@@ -409,7 +447,20 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
 
     // ---- layer 3: 16 -> 1 and the output (TMEM columns 16 t)
     if (tid == 0) issue_tiles<9, 512, 16, false>(tmem, dX, dW3, idesc_n(16), bar_t, 0, kTiles, 0);
-#pragma unroll 1
+    // the output's inputs for this thread's five rows, and the next element's
+    // residual and diagonal, requested before the MMAs are waited for
+    float ojac[kTiles], ow[kTiles];
+#pragma unroll
+    for (int t = 0; t < kTiles; ++t) {
+      const int np = kTile0 + 128 * t + 32 * warp + lane;
+      const int jp = (np >> 3) % 10, kp = np / kPlaneRows;
+      const bool live = jp >= 1 && jp <= kNq;
+      const int n = live ? i + kNq * (jp - 1) + kNq * kNq * (kp - 1) : 0;
+      ojac[t] = ((normalize & kNetAddJacobi) && din) ? din[n] * rin[n] : 0.f;
+      ow[t] = win ? win[n] : 1.f;
+    }
+    load_inputs(e + gridDim.x);
+#pragma unroll
     for (int t = 0; t < kTiles; ++t) {
       ok = wait_tile(t) && ok;
       float v[16];
@@ -424,9 +475,7 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
       const int jp = (np >> 3) % 10, kp = np / kPlaneRows;
       if (jp >= 1 && jp <= kNq) {
         const int n = i + kNq * (jp - 1) + kNq * kNq * (kp - 1);
-        o *= hs[n] * s;
-        if ((normalize & kNetAddJacobi) && din) o += din[n] * rin[n];
-        out[e * kNp + n] = (win ? win[n] : 1.f) * o;
+        out[e * kNp + n] = ow[t] * (o * (hs[n] * s) + ojac[t]);
       }
     }
     ++tphase;
