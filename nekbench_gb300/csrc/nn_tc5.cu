@@ -38,13 +38,10 @@
 //
 // Arithmetic: BF16 weights and activations (the scaled input and both GELU
 // outputs rounded to BF16), FP32 accumulation, the tanh form of GELU with the
-// hardware tanh, evaluated on packed pairs in half precision (its 11-bit
-// significands add less error than the BF16 rounding that follows).  No
-// counterpart in the reference.
+// hardware tanh.  No counterpart in the reference.
 #include "nn.h"
 
 #include <cuda_bf16.h>
-#include <cuda_fp16.h>
 
 namespace nekb {
 namespace {
@@ -142,24 +139,21 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi)
   return *reinterpret_cast<const uint32_t*>(&v);
 }
 
-// GELU (tanh form) of two values, the result rounded to BF16.
-// The tanh argument sqrt(2/pi) x (1 + 0.044715 x^2) and the tanh itself are
-// evaluated in packed half precision (one MUFU operation for both values);
-// the final 0.5 x (1 + tanh) stays in FP32, so the half-precision steps only
-// perturb tanh (error about 1e-4 of the result, below BF16's rounding).  Past
-// |x| = 256 the square overflows to infinity and tanh saturates to +-1, the
-// right limit.
+// GELU (tanh form) of two values with the hardware FP32 tanh, the results
+// packed as BF16.  (Half-precision tanh would halve the MUFU work, but it moves
+// about one activation in eight to the neighbouring BF16 value, which the
+// oracle's FP32 GELU does not.)
+__device__ __forceinline__ float gelu_tc(float x)
+{
+  const float u = 0.7978845608028654f * (x + 0.044715f * x * x * x);
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
+  return 0.5f * x * (1.0f + t);
+}
+
 __device__ __forceinline__ uint32_t gelu2_bf16(float a, float b)
 {
-  const __half2 x = __floats2half2_rn(a, b);
-  const __half2 one = __float2half2_rn(1.0f), c1 = __float2half2_rn(0.044715f);
-  const __half2 c2 = __float2half2_rn(0.7978845608028654f);
-  const __half2 u = __hmul2(__hmul2(x, __hfma2(c1, __hmul2(x, x), one)), c2);
-  __half2 th;
-  asm("tanh.approx.f16x2 %0, %1;" : "=r"(*reinterpret_cast<uint32_t*>(&th)) : "r"(*reinterpret_cast<const uint32_t*>(&u)));
-  const float2 t = __half22float2(th);
-  const float ha = 0.5f * a, hb = 0.5f * b;
-  return pack2(fmaf(ha, t.x, ha), fmaf(hb, t.y, hb));
+  return pack2(gelu_tc(a), gelu_tc(b));
 }
 
 // 16 channels (8 packed BF16 pairs) of one row into an operand buffer
