@@ -54,6 +54,7 @@ constexpr int kRows = 816;               // 8 + 800 + 8 storage rows
 constexpr int kTiles = 5;                // 128-row tiles over padded rows 80..719
 constexpr int kTile0 = kPlaneRows;       // first tile row (plane k' = 1)
 constexpr int kActBytes = kRows * 32;    // one activation buffer
+constexpr int kA0Rows = 10, kA0Plane = 80;  // bordered input: (i + 1) + 10 j + 80 (k + 1)
 
 // shared memory (bytes)
 constexpr int kSmW1 = 0;                         // 3 x [16 n][16 k] bf16
@@ -62,7 +63,7 @@ constexpr int kSmW3 = kSmW2 + 9 * 1536;          // 9 x [16 n][16 k]
 constexpr int kSmX = kSmW3 + 9 * 512;            // layer-1 im2col, then layer-2 output (19968)
 constexpr int kSmY = kSmX + kActBytes;           // layer-1 output
 constexpr int kSmH = kSmY + kActBytes;           // sqrt(invDiag), 512 floats
-constexpr int kSmA0 = kSmH + kNp * 4;            // scaled input (BF16 values), 512 floats
+constexpr int kSmA0 = kSmH + kNp * 4;            // scaled input, BF16, zero-bordered in i and k (800 x 2 bytes)
 constexpr int kSmRed = kSmA0 + kNp * 4;          // block sums
 constexpr int kSmBar = kSmRed + 64;              // 5 tile mbarriers
 constexpr int kSmSlot = kSmBar + kTiles * 8;     // TMEM base address
@@ -139,21 +140,30 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi)
   return *reinterpret_cast<const uint32_t*>(&v);
 }
 
-// GELU (tanh form) of two values with the hardware FP32 tanh, the results
-// packed as BF16.  (Half-precision tanh would halve the MUFU work, but it moves
-// about one activation in eight to the neighbouring BF16 value, which the
-// oracle's FP32 GELU does not.)
-__device__ __forceinline__ float gelu_tc(float x)
+// Twice the GELU (tanh form) of two values, packed as BF16:
+// x (1 + tanh(u)) with u = x (c2 + c3 x^2), c2 = sqrt(2/pi), c3 = 0.044715 c2,
+// with the hardware FP32 tanh.  The factor 1/2 of GELU is carried by the next
+// layer's weights (halved when they are staged; scaling by 2 is exact in BF16,
+// so the products and sums are those of GELU itself).  Half-precision tanh
+// would halve the MUFU work, but it moves about one activation in eight to
+// the neighbouring BF16 value, which the oracle's FP32 GELU does not.
+__device__ __forceinline__ float gelu_x2(float x)
 {
-  const float u = 0.7978845608028654f * (x + 0.044715f * x * x * x);
+  const float u = x * fmaf(0.035677408136300125f, x * x, 0.7978845608028654f);
   float t;
   asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
-  return 0.5f * x * (1.0f + t);
+  return fmaf(x, t, x);
 }
 
 __device__ __forceinline__ uint32_t gelu2_bf16(float a, float b)
 {
-  return pack2(gelu_tc(a), gelu_tc(b));
+  return pack2(gelu_x2(a), gelu_x2(b));
+}
+
+// a BF16 value halved (exact for every normal value)
+__device__ __forceinline__ uint16_t half_bf16(uint16_t v)
+{
+  return (uint16_t)(__float_as_uint(__uint_as_float((uint32_t)v << 16) * 0.5f) >> 16);
 }
 
 // 16 channels (8 packed BF16 pairs) of one row into an operand buffer
@@ -161,22 +171,6 @@ __device__ __forceinline__ void store_row_packed(unsigned char* buf, int row, co
 {
   *reinterpret_cast<uint4*>(buf + core_off(row, 0)) = make_uint4(p[0], p[1], p[2], p[3]);
   *reinterpret_cast<uint4*>(buf + core_off(row, 1)) = make_uint4(p[4], p[5], p[6], p[7]);
-}
-
-// 16 channels of one row into an operand buffer (two 16-byte stores)
-__device__ __forceinline__ void store_row(unsigned char* buf, int row, const float (&v)[16])
-{
-  uint4 lo, hi;
-  lo.x = pack2(v[0], v[1]);
-  lo.y = pack2(v[2], v[3]);
-  lo.z = pack2(v[4], v[5]);
-  lo.w = pack2(v[6], v[7]);
-  hi.x = pack2(v[8], v[9]);
-  hi.y = pack2(v[10], v[11]);
-  hi.z = pack2(v[12], v[13]);
-  hi.w = pack2(v[14], v[15]);
-  *reinterpret_cast<uint4*>(buf + core_off(row, 0)) = lo;
-  *reinterpret_cast<uint4*>(buf + core_off(row, 1)) = hi;
 }
 
 __device__ __forceinline__ void bar_init(uint32_t bar)
@@ -249,7 +243,7 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
   unsigned char* X = smem + kSmX;
   unsigned char* Y = smem + kSmY;
   float* hs = reinterpret_cast<float*>(smem + kSmH);
-  float* a0 = reinterpret_cast<float*>(smem + kSmA0);
+  uint16_t* a0 = reinterpret_cast<uint16_t*>(smem + kSmA0);
   float* red = reinterpret_cast<float*>(smem + kSmRed);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint16_t* W = reinterpret_cast<const uint16_t*>(Wbf);
@@ -266,23 +260,25 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
     }
     *reinterpret_cast<uint16_t*>(smem + kSmW1 + a * 512 + wb_off(co, c)) = v;
   }
+  // layers 2 and 3 take the doubled GELU outputs: their weights are halved
   for (int x = tid; x < 9 * 48 * 16; x += kThreads) {  // W2[(dj,dk)][(di,co)][ci]
     const int b = x / 768, n = (x / 16) % 48, ci = x % 16;
     const int dj = b % 3, dk = b / 3, di = n / 16, co = n % 16;
     const int t = di + 3 * dj + 9 * dk;
-    *reinterpret_cast<uint16_t*>(smem + kSmW2 + b * 1536 + wb_off(n, ci)) = W[kO2 + (co * 16 + ci) * kTaps + t];
+    *reinterpret_cast<uint16_t*>(smem + kSmW2 + b * 1536 + wb_off(n, ci)) = half_bf16(W[kO2 + (co * 16 + ci) * kTaps + t]);
   }
   for (int x = tid; x < 9 * 16 * 16; x += kThreads) {  // W3[(dj,dk)][di][ci], di columns 0..2
     const int b = x / 256, n = (x / 16) % 16, ci = x % 16;
     const int dj = b % 3, dk = b / 3;
     uint16_t v = 0;
-    if (n < 3) v = W[kO3 + ci * kTaps + n + 3 * dj + 9 * dk];
+    if (n < 3) v = half_bf16(W[kO3 + ci * kTaps + n + 3 * dj + 9 * dk]);
     *reinterpret_cast<uint16_t*>(smem + kSmW3 + b * 512 + wb_off(n, ci)) = v;
   }
   for (int x = tid; x < kActBytes / 16; x += kThreads) {
     reinterpret_cast<uint4*>(X)[x] = make_uint4(0, 0, 0, 0);
     reinterpret_cast<uint4*>(Y)[x] = make_uint4(0, 0, 0, 0);
   }
+  for (int x = tid; x < kA0Rows * 8 * kA0Rows; x += kThreads) a0[x] = 0;  // its border stays zero
   if (tid == 0) {
     for (int b = 0; b < kTiles; ++b) bar_init(bar_t + 8 * b);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -328,21 +324,36 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
   };
   load_inputs(blockIdx.x);
 
+  // this thread's tile rows np = kTile0 + 128 t + tid: the node each holds
+  // (i, j'-1, k'-1) as a local index and as its centre in the bordered input;
+  // rows of the padding lines j' = 0, 9 hold no node (bit t of `live` clear)
+  // and are never written after the zeroing above
+  int node[kTiles], ctr[kTiles];
+  unsigned live = 0;
+#pragma unroll
+  for (int t = 0; t < kTiles; ++t) {
+    const int np = kTile0 + 128 * t + tid;
+    const int jp = (np >> 3) % 10, kp = np / kPlaneRows;
+    const bool lv = jp >= 1 && jp <= kNq;
+    live |= (lv ? 1u : 0u) << t;
+    node[t] = lv ? i + kNq * (jp - 1) + kNq * kNq * (kp - 1) : 0;
+    ctr[t] = (i + 1) + kA0Rows * (jp - 1) + kA0Plane * kp;
+  }
+
   for (int64_t e = blockIdx.x; e < Etot; e += gridDim.x) {
     const float* rin = r + e * kNp;
     const float* din = invDiag ? invDiag + (e % Efield) * kNp : nullptr;
     const float* win = w ? w + (e % Efield) * kNp : nullptr;
 
-    // ---- scaled input a0 = bf16(h r / s)
-    float ss = 0.f;
+    // ---- scaled input a0 = bf16(h r / s), into the bordered array
+    float ss = 0.f, vs[kNp / kThreads];
 #pragma unroll
     for (int c = 0; c < kNp / kThreads; ++c) {
       const int n = tid + c * kThreads;
       const float h = din ? sqrtf(nd[c]) : 1.f;
-      const float v = h * nr[c];
+      vs[c] = h * nr[c];
       hs[n] = h;
-      a0[n] = v;
-      ss += v * v;
+      ss += vs[c] * vs[c];
     }
     float s = 1.f;
     if (normalize & kNetNormalize) s = sqrtf(block_sum4(ss, red) / kNp);
@@ -350,30 +361,24 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
 #pragma unroll
     for (int c = 0; c < kNp / kThreads; ++c) {
       const int n = tid + c * kThreads;
-      a0[n] = __bfloat162float(__float2bfloat16_rn(a0[n] * inv));
+      const __nv_bfloat16 b = __float2bfloat16_rn(vs[c] * inv);
+      a0[((n & 7) + 1) + kA0Rows * ((n >> 3) & 7) + kA0Plane * ((n >> 6) + 1)] = *reinterpret_cast<const uint16_t*>(&b);
     }
     __syncthreads();
 
-    // ---- layer-1 operand in X: row (i, j', k') holds the 9 inputs at
-    // (i + di, j' - 1, k' - 1 + dk), column (di + 1) + 3 (dk + 1); rows outside
-    // planes k' = 1..8 stay zero (they are layer 3's zero padding)
-    for (int rs = tid; rs < kRows; rs += kThreads) {
-      const int np = rs - kLead;
-      float v[16];
+    // ---- layer-1 operand in X: tile row (i, j', k') holds the 9 inputs at
+    // (i + di, j' - 1, k' - 1 + dk), column (di + 1) + 3 (dk + 1), read from
+    // the bordered input at offsets di + 80 dk of the node's centre; the other
+    // rows keep their zeros (they are layer 3's zero padding)
 #pragma unroll
-      for (int c = 0; c < 16; ++c) v[c] = 0.f;
-      if (np >= kTile0 && np < kTile0 + kTiles * 128) {
-        const int ii = np & 7, jj = ((np >> 3) % 10) - 1, kk = np / kPlaneRows - 1;
-        if (jj >= 0 && jj < kNq) {
-#pragma unroll
-          for (int c = 0; c < 9; ++c) {
-            const int di = c % 3 - 1, dk = c / 3 - 1;
-            const int a = ii + di, b = kk + dk;
-            if (a >= 0 && a < kNq && b >= 0 && b < kNq) v[c] = a0[a + kNq * jj + kNq * kNq * b];
-          }
-        }
-      }
-      store_row(X, rs, v);
+    for (int t = 0; t < kTiles; ++t) {
+      if (!((live >> t) & 1u)) continue;
+      const uint16_t* q = a0 + ctr[t];
+      const int row = kLead + kTile0 + 128 * t + tid;
+      *reinterpret_cast<uint4*>(X + core_off(row, 0)) =
+          make_uint4(q[-81] | (uint32_t)q[-80] << 16, q[-79] | (uint32_t)q[-1] << 16, q[0] | (uint32_t)q[1] << 16,
+                     q[79] | (uint32_t)q[80] << 16);
+      *reinterpret_cast<uint4*>(X + core_off(row, 1)) = make_uint4(q[81], 0u, 0u, 0u);
     }
     fence_async_smem();
     fence_before();
@@ -388,13 +393,10 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
       float v[16];
       ld16(tlane + (uint32_t)(16 * t), v);
       ld_wait();
-      const int np = kTile0 + 128 * t + 32 * warp + lane;
-      const int jp = (np >> 3) % 10;
-      const bool live = jp >= 1 && jp <= kNq;
       uint32_t g[8];
 #pragma unroll
-      for (int c = 0; c < 8; ++c) g[c] = live ? gelu2_bf16(v[2 * c], v[2 * c + 1]) : 0u;
-      store_row_packed(Y, np + kLead, g);
+      for (int c = 0; c < 8; ++c) g[c] = gelu2_bf16(v[2 * c], v[2 * c + 1]);
+      if ((live >> t) & 1u) store_row_packed(Y, kLead + kTile0 + 128 * t + tid, g);
     }
     ++tphase;
     fence_async_smem();
@@ -418,9 +420,6 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
         __syncthreads();
         if (tid == 0) issue_tiles<9, 1536, 48, false>(tmem, dY, dW2, idesc_n(48), bar_t, t + 2, t + 3, 2);
       }
-      const int np = kTile0 + 128 * t + 32 * warp + lane;
-      const int jp = (np >> 3) % 10;
-      const bool live = jp >= 1 && jp <= kNq;
 #pragma unroll
       for (int c = 0; c < 16; ++c) {
         const float up = __shfl_down_sync(0xffffffffu, vp[c], 1);  // node i + 1, column di = +1
@@ -432,8 +431,8 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
       }
       uint32_t g[8];
 #pragma unroll
-      for (int c = 0; c < 8; ++c) g[c] = live ? gelu2_bf16(v0[2 * c], v0[2 * c + 1]) : 0u;
-      store_row_packed(X, np + kLead, g);
+      for (int c = 0; c < 8; ++c) g[c] = gelu2_bf16(v0[2 * c], v0[2 * c + 1]);
+      if ((live >> t) & 1u) store_row_packed(X, kLead + kTile0 + 128 * t + tid, g);
     }
     ++tphase;
     fence_async_smem();
@@ -447,10 +446,7 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
     float ojac[kTiles], ow[kTiles];
 #pragma unroll
     for (int t = 0; t < kTiles; ++t) {
-      const int np = kTile0 + 128 * t + 32 * warp + lane;
-      const int jp = (np >> 3) % 10, kp = np / kPlaneRows;
-      const bool live = jp >= 1 && jp <= kNq;
-      const int n = live ? i + kNq * (jp - 1) + kNq * kNq * (kp - 1) : 0;
+      const int n = node[t];
       ojac[t] = ((normalize & kNetAddJacobi) && din) ? din[n] * rin[n] : 0.f;
       ow[t] = win ? win[n] : 1.f;
     }
@@ -466,10 +462,8 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
       float o = v[1];
       if (i < kNq - 1) o += up;
       if (i > 0) o += dn;
-      const int np = kTile0 + 128 * t + 32 * warp + lane;
-      const int jp = (np >> 3) % 10, kp = np / kPlaneRows;
-      if (jp >= 1 && jp <= kNq) {
-        const int n = i + kNq * (jp - 1) + kNq * kNq * (kp - 1);
+      if ((live >> t) & 1u) {
+        const int n = node[t];
         out[e * kNp + n] = ow[t] * (o * (hs[n] * s) + ojac[t]);
       }
     }
