@@ -78,8 +78,12 @@ struct nekb_bp {
   // reduction scratch and solver state
   nekb::DeviceBuf partials, counter, state;
   nekb::PcgState* h_state = nullptr;  // pinned mirror
-  // CUDA graphs of one chunk of PCG iterations, keyed by their arguments
-  std::map<std::tuple<int, int, int, const void*, const void*, const void*, int>, cudaGraphExec_t> graphs;
+  // CUDA graphs of one chunk of PCG iterations, keyed by their arguments and,
+  // with the learned preconditioner, by the network, its weights' address and
+  // the inference kernel it runs (a graph replays the launches it captured)
+  std::map<std::tuple<int, int, int, const void*, const void*, const void*, int, const void*, const void*, int>,
+           cudaGraphExec_t>
+      graphs;
   void* net = nullptr;  // learned preconditioner in use (nekb_net*)
 };
 

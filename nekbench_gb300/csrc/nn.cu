@@ -605,6 +605,15 @@ int net_infer(const nekb_net* net, int64_t Etot, int64_t Efield, const float* r,
   NEKB_NET_DISPATCH(run_infer, net, Etot, Efield, r, w, invDiag, out, normalize, skip, s)
 }
 
+// the kernel net_infer launches: 0 FP32 cores, else the tensor-core mode
+int resolved_mode(const nekb_net* net)
+{
+  const int mode = net->inference == NEKB_NET_TENSOR ? kTensorDefault : net->inference;
+  if ((mode == NEKB_NET_TENSOR_TC5 || mode == NEKB_NET_TENSOR_SYNC) && net_tc_supported(net->Nq, net->C))
+    return mode;
+  return NEKB_NET_FP32;
+}
+
 int net_train(nekb_net* net, int64_t E, const float* in, const float* target, cudaStream_t s)
 {
   NEKB_NET_DISPATCH(run_train, net, E, in, target, s)
@@ -617,6 +626,12 @@ bool net_supported(int Nq, int C)
 }
 
 }  // namespace
+
+NetSignature net_signature(const nekb_net* net)
+{
+  if (!net) return NetSignature{nullptr, nullptr, 0};
+  return NetSignature{net, net->Wbf.p, (net->Nq * 100 + net->C) * 8 + resolved_mode(net)};
+}
 
 int net_precondition(nekb_bp* bp, nekb_net* net, const float* r, float* z, const float* invDiag,
                      const float* w, const int* skip, cudaStream_t s)

@@ -13,6 +13,15 @@ namespace nekb {
 int net_precondition(nekb_bp* bp, nekb_net* net, const float* r, float* z, const float* invDiag,
                      const float* w, const int* skip, cudaStream_t s);
 
+// what a captured PCG graph bakes in from the network: its order, channels,
+// the inference kernel that runs (the resolved mode) and its weights' address
+struct NetSignature {
+  const void* net;
+  const void* weights;
+  int shape_mode;  // (Nq * 100 + C) * 8 + resolved mode
+};
+NetSignature net_signature(const nekb_net* net);
+
 // inference mode bits: normalise by the element RMS of sqrt(invDiag) r; add
 // w invDiag r to the output
 constexpr int kNetNormalize = 1, kNetAddJacobi = 2;

@@ -31,10 +31,12 @@
 // epilogue of tile t (TMEM -> registers, shuffles, GELU, BF16, next layer's
 // operand) overlaps the MMAs of the later tiles.  Layer 2's accumulators
 // (5 tiles x 48 columns) cycle through two 48-column buffers: tile t + 2 is
-// issued once every warp has read tile t.  Inputs are read straight from
-// global memory.  Every wait is bounded; a wait that runs out sets a device
-// flag, the CTA waits (bounded) for its operations in flight, frees its TMEM
-// and returns.
+// issued once every warp has read tile t.  The input staging is bordered with
+// zeros in i and k, so the layer-1 im2col reads its nine taps without bounds
+// tests; GELU's factor 1/2 rides in the next layer's weights (halved when
+// staged).  Inputs are read straight from global memory.  Every wait is
+// bounded; a wait that runs out sets a device flag, the CTA waits (bounded)
+// for its operations in flight, frees its TMEM and returns.
 //
 // Arithmetic: BF16 weights and activations (the scaled input and both GELU
 // outputs rounded to BF16), FP32 accumulation, the tanh form of GELU with the
@@ -475,7 +477,7 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
   if (failed) {  // flag, then wait (bounded) for this CTA's MMAs in flight
     if (tid == 0) {
       atomicExch(&g_tc5_timeout, 1);
-      for (int t = 0; t < kTiles; ++t) bar_wait(bar_t + 8 * t, tphase & 1u);
+      for (int t = 0; t < kTiles; ++t) bar_wait(bar_t + 8 * t, (tphase - 1u) & 1u);  // the layer that stopped
     }
     fence_before();
     __syncthreads();

@@ -837,9 +837,10 @@ int pcg_core(nekb_bp* bp, const OpView& op, T* r, T* x, const T* w, const T* inv
   if (chunk < 1) chunk = 1;
   cudaGraphExec_t gexec = nullptr;
   if (use_graph) {
+    const NetSignature ns = net_signature(ext ? ext->net : nullptr);
     auto key = std::make_tuple(op.precision * 64 + mode * 4 + (flex ? 2 : 0) + (int)(sizeof(T) == 8),
                                chunk, op.flags, (const void*)op.lambda, (const void*)r, (const void*)x,
-                               (int)(ext && ext->net ? 1 + ext->m : 0));
+                               (int)(ext && ext->net ? 1 + ext->m : 0), ns.net, ns.weights, ns.shape_mode);
     auto it = bp->graphs.find(key);
     if (it != bp->graphs.end()) {
       gexec = it->second;

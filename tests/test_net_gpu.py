@@ -220,6 +220,51 @@ def test_learned_solve_on_tcgen05_kernel(nb, O, dev):
     assert abs(its[nb.NET_TENSOR_TC5] - its[nb.NET_TENSOR_SYNC]) <= 0.1 * its[nb.NET_TENSOR_SYNC] + 5, its
 
 
+def test_captured_solver_graph_follows_the_network(nb, O, dev):
+    """The solver replays one captured CUDA graph per chunk of iterations and
+    keeps it for the next solve with the same arguments.  A solve on the same
+    problem and buffers with another network, or with the same network on the
+    other inference kernel, runs that network: its iterates equal those of a
+    fresh problem object that never saw the first network."""
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                        "nekbench_gb300", "weights", "precond_n7_c16.bin")
+    trained = nb.Net.load(path)
+    other = nb.Net.load(path)
+    w = np.asarray(other.weights(), np.float32).copy()
+    w[27 * 16:] *= -0.5  # another network: layers 2 and 3 changed
+    other.set_weights(w)
+
+    def make():
+        bp = nb.BP(7, 3, 3, 3, perturb=0.1, seed=3)
+        L = bp.Nlocal
+        lam = torch.cat([torch.full((L,), 1.0), torch.full((L,), 1.5)]).double().to(dev)
+        f = torch.from_numpy(O.uniform(L, 8, 3, -1, 1)).to(dev)
+        bp.ogs.gather_scatter_many(f)
+        return bp, lam, f
+
+    def solve(bp, lam, f, r, x, net, mode):
+        net.inference = mode
+        r.copy_(f)
+        x.zero_()
+        bp.pcg(lam, r, x, 1e-12, 24, solver=nb.SOLVER_MIXED, precond=nb.PRECOND_LEARNED, net=net,
+               fixed_iterations=True)
+        torch.cuda.synchronize()
+        return x.clone()
+
+    bp, lam, f = make()
+    r, x = torch.empty_like(f), torch.empty_like(f)
+    runs = [(trained, nb.NET_TENSOR_TC5), (other, nb.NET_TENSOR_TC5), (trained, nb.NET_TENSOR_SYNC),
+            (trained, nb.NET_FP32)]
+    shared = [solve(bp, lam, f, r, x, net, mode) for net, mode in runs]
+    for (net, mode), got in zip(runs, shared):
+        bp2, lam2, f2 = make()
+        want = solve(bp2, lam2, f2, torch.empty_like(f2), torch.empty_like(f2), net, mode)
+        assert torch.equal(got, want), (mode, float((got - want).abs().max()))
+    # the runs differ from one another, so a replayed graph would have shown
+    assert not torch.equal(shared[0], shared[1])
+    assert not torch.equal(shared[0], shared[3])
+
+
 def test_inference_mode_falls_back_where_not_built(nb):
     net = nb.Net(4, 8, 3, seed=1)
     assert net.inference == nb.NET_FP32
