@@ -57,8 +57,7 @@ int apply_op(const OpView& op, const void* q, void* Aq, const int* skip, cudaStr
   NEKB_TRY(launch_axhelm(op.Nq, op.flags, op.precision, a, s));
   const bool fp64 = op.precision == NEKB_FP64 || op.precision == NEKB_FP64_SPLIT;
   const int dtype = fp64 ? NEKB_DOUBLE : NEKB_FLOAT;
-  NEKB_TRY(launch_gs_add(op.ogs->Nmulti, op.ogs->d_offsets, op.ogs->d_ids, op.Nfields, op.offset,
-                         Aq, dtype, skip, s));
+  NEKB_TRY(launch_gs_add(op.ogs, op.Nfields, op.offset, Aq, dtype, skip, s));
   NEKB_TRY(launch_mask(op.Nmasked, op.mask, op.Nfields, op.offset, Aq, dtype, skip, s));
   return NEKB_OK;
 }
@@ -320,6 +319,8 @@ nekb_bp* nekb_bp_create_mesh(int N, int64_t E, int Nfields, const double* ggeo, 
 void nekb_ogs_release(nekb_ogs* o)
 {
   if (!o) return;
+  cudaFree(o->d_pairs);
+  cudaFree(o->d_quads);
   cudaFree(o->d_offsets);
   cudaFree(o->d_ids);
   cudaFree(o->d_invDegree);

@@ -216,8 +216,7 @@ int nekb_ogs_gs_many(nekb_ogs* ogs, void* v, int k, int64_t stride, int dtype, i
   if (op != NEKB_OP_ADD) return fail(NEKB_ERR_UNSUPPORTED, "gs: only the add operation is supported");
   if (k < 1 || (k > 1 && stride < ogs->N)) return fail(NEKB_ERR_INVALID, "gs: k=%d stride=%lld", k, (long long)stride);
   if (!v && ogs->Nmulti > 0) return fail(NEKB_ERR_INVALID, "gs: NULL vector");
-  return launch_gs_add(ogs->Nmulti, ogs->d_offsets, ogs->d_ids, k, stride, v, dtype, nullptr,
-                       static_cast<cudaStream_t>(stream));
+  return launch_gs_add(ogs, k, stride, v, dtype, nullptr, static_cast<cudaStream_t>(stream));
 }
 
 int nekb_ogs_sizes(const nekb_ogs* ogs, int64_t* s)

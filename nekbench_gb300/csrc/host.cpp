@@ -209,22 +209,30 @@ int nekb_ogs_build(nekb_ogs* o, int64_t N, const int64_t* ids)
     const double v = 1.0 / (double)(e - s);
     for (int32_t n = s; n < e; ++n) invdeg[o->h_ids[n]] = v;
   }
-  // compact CSR of the groups with more than one member, for the device kernel
-  std::vector<int32_t> moff(1, 0), mids;
-  mids.reserve(Nl);
+  // the groups with more than one member, for the device kernel: groups of
+  // two and of four as packed member ids, the others as a compact CSR
+  std::vector<int32_t> pairs, quads, moff(1, 0), mids;
   for (int64_t q = 0; q < Ng; ++q) {
     const int32_t s = o->h_offsets[q], e = o->h_offsets[q + 1];
     if (e - s < 2) continue;
-    for (int32_t n = s; n < e; ++n) mids.push_back(o->h_ids[n]);
-    moff.push_back((int32_t)mids.size());
+    std::vector<int32_t>& dst = e - s == 2 ? pairs : (e - s == 4 ? quads : mids);
+    for (int32_t n = s; n < e; ++n) dst.push_back(o->h_ids[n]);
+    if (e - s != 2 && e - s != 4) moff.push_back((int32_t)mids.size());
   }
-  o->Nmulti = (int64_t)moff.size() - 1;
-  NEKB_CUDA(cudaMalloc(&o->d_offsets, sizeof(int32_t) * moff.size()));
-  NEKB_CUDA(cudaMemcpy(o->d_offsets, moff.data(), sizeof(int32_t) * moff.size(), cudaMemcpyHostToDevice));
-  if (!mids.empty()) {
-    NEKB_CUDA(cudaMalloc(&o->d_ids, sizeof(int32_t) * mids.size()));
-    NEKB_CUDA(cudaMemcpy(o->d_ids, mids.data(), sizeof(int32_t) * mids.size(), cudaMemcpyHostToDevice));
-  }
+  o->Npairs = (int64_t)pairs.size() / 2;
+  o->Nquads = (int64_t)quads.size() / 4;
+  o->Nrest = (int64_t)moff.size() - 1;
+  o->Nmulti = o->Npairs + o->Nquads + o->Nrest;
+  auto upload = [](int32_t** d, const std::vector<int32_t>& h) -> int {
+    if (h.empty()) return NEKB_OK;
+    NEKB_CUDA(cudaMalloc(d, sizeof(int32_t) * h.size()));
+    NEKB_CUDA(cudaMemcpy(*d, h.data(), sizeof(int32_t) * h.size(), cudaMemcpyHostToDevice));
+    return NEKB_OK;
+  };
+  NEKB_TRY(upload(&o->d_pairs, pairs));
+  NEKB_TRY(upload(&o->d_quads, quads));
+  NEKB_TRY(upload(&o->d_offsets, moff));
+  NEKB_TRY(upload(&o->d_ids, mids));
   if (N > 0) {
     NEKB_CUDA(cudaMalloc(&o->d_invDegree, sizeof(double) * N));
     NEKB_CUDA(cudaMemcpy(o->d_invDegree, invdeg.data(), sizeof(double) * N, cudaMemcpyHostToDevice));

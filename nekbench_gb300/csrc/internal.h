@@ -105,8 +105,10 @@ int launch_physical_nodes(int Nq, int64_t E, const double* EX, const double* EY,
                           const double* r1d, double* x, double* y, double* z, cudaStream_t s);
 
 // ---------------------------------------------------------------- gather-scatter
-int launch_gs_add(int64_t Ngroups, const int32_t* offsets, const int32_t* ids, int k,
-                  int64_t stride, void* q, int dtype, const int* skip, cudaStream_t s);
+// gatherScatterMany add over the multi-member groups of `ogs` (k fields of the
+// given stride)
+int launch_gs_add(const nekb_ogs* ogs, int k, int64_t stride, void* q, int dtype, const int* skip,
+                  cudaStream_t s);
 int launch_mask(int64_t Nmasked, const int32_t* ids, int k, int64_t stride, void* q, int dtype,
                 const int* skip, cudaStream_t s);
 
@@ -129,7 +131,13 @@ struct nekb_ogs {
   int64_t Nmulti = 0;                 // groups with more than one member
   std::vector<int32_t> h_offsets;     // NlocalGather+1 (reference CSR, host)
   std::vector<int32_t> h_ids;         // Nlocal
-  int32_t* d_offsets = nullptr;       // Nmulti+1  (multi-member groups only)
-  int32_t* d_ids = nullptr;           // members of multi-member groups
+  // device copy of the multi-member groups by size: groups of two and of four
+  // as packed member ids (a box mesh's face and edge nodes), every other size
+  // as CSR; members in CSR order within each group
+  int64_t Npairs = 0, Nquads = 0, Nrest = 0;
+  int32_t* d_pairs = nullptr;         // 2 Npairs
+  int32_t* d_quads = nullptr;         // 4 Nquads
+  int32_t* d_offsets = nullptr;       // Nrest+1
+  int32_t* d_ids = nullptr;           // members of the other groups
   double* d_invDegree = nullptr;      // N
 };

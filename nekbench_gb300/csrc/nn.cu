@@ -627,6 +627,21 @@ bool net_supported(int Nq, int C)
 
 }  // namespace
 
+bool net_takes_update(const nekb_net* net) { return net && resolved_mode(net) == NEKB_NET_TENSOR_TC5; }
+
+int net_precondition_update(nekb_bp* bp, nekb_net* net, const NetUpdate& up, float* r, float* z,
+                            const float* invDiag, const float* w, const int* skip, cudaStream_t s)
+{
+  if (!net_takes_update(net)) return fail(NEKB_ERR_UNSUPPORTED, "net: the folded update needs the tcgen05 kernel");
+  if (net->Nq != bp->Nq) return fail(NEKB_ERR_INVALID, "net order Nq=%d differs from the mesh's %d", net->Nq, bp->Nq);
+  NEKB_TRY(net_infer_tc5(net->Wbf.as<__nv_bfloat16>(), bp->Nfields * bp->E, bp->E, r, w, invDiag, z,
+                         kNetNormalize | kNetAddJacobi, skip, s, &up));
+  NEKB_TRY(launch_gs_add(bp->ogs, bp->Nfields, bp->offset, z, NEKB_FLOAT, skip, s));
+  NEKB_TRY(launch_mask(bp->Nmasked, bp->mask.as<int32_t>(), bp->Nfields, bp->offset, z, NEKB_FLOAT,
+                       skip, s));
+  return NEKB_OK;
+}
+
 NetSignature net_signature(const nekb_net* net)
 {
   if (!net) return NetSignature{nullptr, nullptr, 0};
@@ -641,8 +656,7 @@ int net_precondition(nekb_bp* bp, nekb_net* net, const float* r, float* z, const
   // z = w (h s net + invDiag r) per element copy, then assembled and masked
   NEKB_TRY(net_infer(net, bp->Nfields * bp->E, bp->E, r, w, invDiag, z,
                      kNetNormalize | kNetAddJacobi, skip, s));
-  NEKB_TRY(launch_gs_add(bp->ogs->Nmulti, bp->ogs->d_offsets, bp->ogs->d_ids, bp->Nfields,
-                         bp->offset, z, NEKB_FLOAT, skip, s));
+  NEKB_TRY(launch_gs_add(bp->ogs, bp->Nfields, bp->offset, z, NEKB_FLOAT, skip, s));
   NEKB_TRY(launch_mask(bp->Nmasked, bp->mask.as<int32_t>(), bp->Nfields, bp->offset, z, NEKB_FLOAT,
                        skip, s));
   return NEKB_OK;

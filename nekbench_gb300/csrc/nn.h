@@ -13,6 +13,22 @@ namespace nekb {
 int net_precondition(nekb_bp* bp, nekb_net* net, const float* r, float* z, const float* invDiag,
                      const float* w, const int* skip, cudaStream_t s);
 
+// The flexible CG's update folded into the tcgen05 network kernel: before an
+// element is evaluated, r_e -= alpha Ap_e (written back to r) and
+// x_e += alpha p_e, with alpha = (float) *alpha read on the device -- the
+// arithmetic of the separate update pass.
+struct NetUpdate {
+  const double* alpha;
+  const float* Ap;
+  const float* p;
+  float* x;
+};
+// whether net_precondition_update can fold the update (the tcgen05 kernel runs)
+bool net_takes_update(const nekb_net* net);
+// the update above, then net_precondition on the updated r
+int net_precondition_update(nekb_bp* bp, nekb_net* net, const NetUpdate& up, float* r, float* z,
+                            const float* invDiag, const float* w, const int* skip, cudaStream_t s);
+
 // what a captured PCG graph bakes in from the network: its order, channels,
 // the inference kernel that runs (the resolved mode) and its weights' address
 struct NetSignature {
@@ -31,7 +47,7 @@ constexpr int kNetNormalize = 1, kNetAddJacobi = 2;
 bool net_tc_supported(int Nq, int C);
 int net_infer_tc5(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const float* r,
                   const float* w, const float* invDiag, float* out, int normalize, const int* skip,
-                  cudaStream_t s);
+                  cudaStream_t s, const NetUpdate* up = nullptr);
 int net_infer_tc(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const float* r,
                  const float* w, const float* invDiag, float* out, int normalize, const int* skip,
                  cudaStream_t s);

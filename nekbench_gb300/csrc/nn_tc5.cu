@@ -142,24 +142,51 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi)
   return *reinterpret_cast<const uint32_t*>(&v);
 }
 
-// Twice the GELU (tanh form) of two values, packed as BF16:
-// x (1 + tanh(u)) with u = x (c2 + c3 x^2), c2 = sqrt(2/pi), c3 = 0.044715 c2,
-// with the hardware FP32 tanh.  The factor 1/2 of GELU is carried by the next
-// layer's weights (halved when they are staged; scaling by 2 is exact in BF16,
-// so the products and sums are those of GELU itself).  Half-precision tanh
-// would halve the MUFU work, but it moves about one activation in eight to
-// the neighbouring BF16 value, which the oracle's FP32 GELU does not.
-__device__ __forceinline__ float gelu_x2(float x)
+// Packed FP32 pairs: two independent round-to-nearest operations in one
+// instruction, bit for bit the scalar operations.
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c)
 {
-  const float u = x * fmaf(0.035677408136300125f, x * x, 0.7978845608028654f);
-  float t;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
-  return fmaf(x, t, x);
+  float2 d;
+  asm("{\n .reg .b64 ra, rb, rc, rd;\n mov.b64 ra, {%2, %3};\n mov.b64 rb, {%4, %5};\n mov.b64 rc, {%6, %7};\n"
+      " fma.rn.f32x2 rd, ra, rb, rc;\n mov.b64 {%0, %1}, rd;\n}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
 }
 
+__device__ __forceinline__ float2 mul2(float2 a, float2 b)
+{
+  float2 d;
+  asm("{\n .reg .b64 ra, rb, rd;\n mov.b64 ra, {%2, %3};\n mov.b64 rb, {%4, %5};\n"
+      " mul.rn.f32x2 rd, ra, rb;\n mov.b64 {%0, %1}, rd;\n}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+
+__device__ __forceinline__ float tanh_approx(float u)
+{
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(u));
+  return t;
+}
+
+// Twice the GELU (tanh form) of two values, packed as BF16:
+// x (1 + tanh(u)) with u = x (c2 + c3 x^2), c2 = sqrt(2/pi), c3 = 0.044715 c2,
+// with the hardware FP32 tanh and the products on packed pairs.  The factor
+// 1/2 of GELU is carried by the next layer's weights (halved when they are
+// staged; scaling by 2 is exact in BF16, so the products and sums are those
+// of GELU itself).  Half-precision tanh would halve the MUFU work, but it
+// moves about one activation in eight to the neighbouring BF16 value, which
+// the oracle's FP32 GELU does not.
 __device__ __forceinline__ uint32_t gelu2_bf16(float a, float b)
 {
-  return pack2(gelu_x2(a), gelu_x2(b));
+  const float2 x = make_float2(a, b);
+  const float2 p = fma2(make_float2(0.035677408136300125f, 0.035677408136300125f), mul2(x, x),
+                        make_float2(0.7978845608028654f, 0.7978845608028654f));
+  const float2 u = mul2(x, p);
+  const float2 g = fma2(x, make_float2(tanh_approx(u.x), tanh_approx(u.y)), x);
+  return pack2(g.x, g.y);
 }
 
 // a BF16 value halved (exact for every normal value)
@@ -235,12 +262,17 @@ __device__ __forceinline__ void issue_tiles(uint32_t tmem, uint64_t da, uint64_t
 // ((n/8)*2 + k/8)*128 + (n%8)*16 + (k%8)*2
 __device__ __forceinline__ int wb_off(int n, int k) { return ((n >> 3) * 2 + (k >> 3)) * 128 + (n & 7) * 16 + (k & 7) * 2; }
 
+// UPDATE: the flexible CG's update is applied first, element by element:
+// r -= alpha Ap (written back to r, from which the output's Jacobi term then
+// reads) and x += alpha p
+template <bool UPDATE>
 __global__ void __launch_bounds__(kThreads, kCtasPerSm)
-k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ Wbf,
-                const float* __restrict__ r, const float* __restrict__ w, const float* __restrict__ invDiag,
-                float* __restrict__ out, int normalize, const int* skip)
+k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ Wbf, float* r,
+                const float* __restrict__ w, const float* __restrict__ invDiag, float* __restrict__ out,
+                int normalize, const int* skip, NetUpdate up)
 {
   if (skip != nullptr && *skip != 0) return;
+  const float alpha = UPDATE ? (float)*up.alpha : 0.f;
   extern __shared__ __align__(1024) unsigned char smem[];
   unsigned char* X = smem + kSmX;
   unsigned char* Y = smem + kSmY;
@@ -313,15 +345,22 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
     return ok;
   };
 
-  // this thread's residual and diagonal values of the element it starts next,
-  // loaded one element ahead (nodes tid + 128 c)
-  float nr[kNp / kThreads], nd[kNp / kThreads];
+  // this thread's residual and diagonal values of the element it starts next
+  // (and with UPDATE its A p, p and x values), loaded one element ahead
+  // (nodes tid + 128 c)
+  float nr[kNp / kThreads], nd[kNp / kThreads], nap[kNp / kThreads], npv[kNp / kThreads],
+      nxv[kNp / kThreads];
   auto load_inputs = [&](int64_t el) {
 #pragma unroll
     for (int c = 0; c < kNp / kThreads; ++c) {
       const int n = tid + c * kThreads;
       nr[c] = el < Etot ? r[el * kNp + n] : 0.f;
       nd[c] = (el < Etot && invDiag) ? invDiag[(el % Efield) * kNp + n] : 1.f;
+      if (UPDATE) {
+        nap[c] = el < Etot ? up.Ap[el * kNp + n] : 0.f;
+        npv[c] = el < Etot ? up.p[el * kNp + n] : 0.f;
+        nxv[c] = el < Etot ? up.x[el * kNp + n] : 0.f;
+      }
     }
   };
   load_inputs(blockIdx.x);
@@ -352,6 +391,11 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
 #pragma unroll
     for (int c = 0; c < kNp / kThreads; ++c) {
       const int n = tid + c * kThreads;
+      if (UPDATE) {  // the update pass's r -= alpha Ap and x += alpha p
+        nr[c] = fmaf(-alpha, nap[c], nr[c]);
+        r[e * kNp + n] = nr[c];
+        up.x[e * kNp + n] = fmaf(alpha, npv[c], nxv[c]);
+      }
       const float h = din ? sqrtf(nd[c]) : 1.f;
       vs[c] = h * nr[c];
       hs[n] = h;
@@ -422,14 +466,19 @@ k_net_infer_tc5(int64_t Etot, int64_t Efield, const __nv_bfloat16* __restrict__ 
         __syncthreads();
         if (tid == 0) issue_tiles<9, 1536, 48, false>(tmem, dY, dW2, idesc_n(48), bar_t, t + 2, t + 3, 2);
       }
+      // out(i) = V(i)[0] + V(i + 1)[+1] + V(i - 1)[-1], the neighbours' terms
+      // taken inside the element only (a factor 1 or 0: 1 x + o rounds as o + x)
+      const float2 fu = make_float2(i < kNq - 1 ? 1.f : 0.f, i < kNq - 1 ? 1.f : 0.f);
+      const float2 fd = make_float2(i > 0 ? 1.f : 0.f, i > 0 ? 1.f : 0.f);
 #pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        const float up = __shfl_down_sync(0xffffffffu, vp[c], 1);  // node i + 1, column di = +1
-        const float dn = __shfl_up_sync(0xffffffffu, vm[c], 1);    // node i - 1, column di = -1
-        float o = v0[c];
-        if (i < kNq - 1) o += up;
-        if (i > 0) o += dn;
-        v0[c] = o;
+      for (int c = 0; c < 16; c += 2) {
+        const float2 up = make_float2(__shfl_down_sync(0xffffffffu, vp[c], 1),  // node i + 1, column di = +1
+                                      __shfl_down_sync(0xffffffffu, vp[c + 1], 1));
+        const float2 dn = make_float2(__shfl_up_sync(0xffffffffu, vm[c], 1),  // node i - 1, column di = -1
+                                      __shfl_up_sync(0xffffffffu, vm[c + 1], 1));
+        const float2 o = fma2(dn, fd, fma2(up, fu, make_float2(v0[c], v0[c + 1])));
+        v0[c] = o.x;
+        v0[c + 1] = o.y;
       }
       uint32_t g[8];
 #pragma unroll
@@ -508,10 +557,15 @@ int net_tc5_raise_timeout()
 }
 
 int net_infer_tc5(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const float* r, const float* w,
-                  const float* invDiag, float* out, int normalize, const int* skip, cudaStream_t s)
+                  const float* invDiag, float* out, int normalize, const int* skip, cudaStream_t s,
+                  const NetUpdate* up)
 {
-  static SmemOptIn smem_opt;
-  NEKB_TRY(smem_opt.ensure(k_net_infer_tc5, kSmTotal));
+  static SmemOptIn smem_plain, smem_update;
+  if (up) {
+    NEKB_TRY(smem_update.ensure(k_net_infer_tc5<true>, kSmTotal));
+  } else {
+    NEKB_TRY(smem_plain.ensure(k_net_infer_tc5<false>, kSmTotal));
+  }
   int dev = 0, sms = 152;
   NEKB_CUDA(cudaGetDevice(&dev));
   NEKB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -521,8 +575,14 @@ int net_infer_tc5(const __nv_bfloat16* Wbf, int64_t Etot, int64_t Efield, const 
   int64_t grid = (int64_t)sms * kCtasPerSm;
   if (grid > Etot) grid = Etot;
   if (grid < 1) return NEKB_OK;
-  k_net_infer_tc5<<<(unsigned)grid, kThreads, kSmTotal, s>>>(Etot, Efield, Wbf, r, w, invDiag, out,
-                                                              normalize, skip);
+  // r is written only with the update, which the caller passes a writable r for
+  float* rw = const_cast<float*>(r);
+  if (up)
+    k_net_infer_tc5<true><<<(unsigned)grid, kThreads, kSmTotal, s>>>(Etot, Efield, Wbf, rw, w, invDiag, out,
+                                                                     normalize, skip, *up);
+  else
+    k_net_infer_tc5<false><<<(unsigned)grid, kThreads, kSmTotal, s>>>(Etot, Efield, Wbf, rw, w, invDiag,
+                                                                      out, normalize, skip, NetUpdate{});
   NEKB_CUDA(cudaGetLastError());
   return NEKB_OK;
 }

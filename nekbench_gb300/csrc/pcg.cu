@@ -678,9 +678,14 @@ int launch_fcg_iteration(const OpView& op, PcgArgs<T> a, const ExtPrecond* ext, 
       k_fcg_pap<T, 1><<<red_grid(a.Nloc), RT, 0, s>>>(a, ext->AP, Nall);
     }
     NEKB_CUDA(cudaGetLastError());
-    k_update<T><<<vec_grid(Nall), RT, 0, s>>>(a);
-    NEKB_CUDA(cudaGetLastError());
-    NEKB_TRY(net_precondition(ext->bp, ext->net, a.r, a.z, ext->invDiag, ext->w, &a.st->done, s));
+    if (net_takes_update(ext->net)) {  // x += alpha p, r -= alpha Ap inside the network kernel
+      const NetUpdate up{&a.st->alpha, a.Ap, a.p, a.x};
+      NEKB_TRY(net_precondition_update(ext->bp, ext->net, up, a.r, a.z, ext->invDiag, ext->w, &a.st->done, s));
+    } else {
+      k_update<T><<<vec_grid(Nall), RT, 0, s>>>(a);
+      NEKB_CUDA(cudaGetLastError());
+      NEKB_TRY(net_precondition(ext->bp, ext->net, a.r, a.z, ext->invDiag, ext->w, &a.st->done, s));
+    }
     return launch_fcg_dots<T, false>(a, ext, s);
   } else {
     return fail(NEKB_ERR_UNSUPPORTED, "FCG(m) runs in FP32 only");
@@ -723,10 +728,15 @@ int launch_iteration(const OpView& op, PcgArgs<T> a, int mode, bool flex, const 
   }
   NEKB_CUDA(cudaGetLastError());
   if (mode == PC_EXTERNAL) {
-    k_update<T><<<vec_grid(Nall), RT, 0, s>>>(a);
-    NEKB_CUDA(cudaGetLastError());
     if constexpr (sizeof(T) == 4) {
-      NEKB_TRY(net_precondition(ext->bp, ext->net, a.r, a.z, ext->invDiag, ext->w, &a.st->done, s));
+      if (net_takes_update(ext->net)) {  // x += alpha p, r -= alpha Ap inside the network kernel
+        const NetUpdate up{&a.st->alpha, a.Ap, a.p, a.x};
+        NEKB_TRY(net_precondition_update(ext->bp, ext->net, up, a.r, a.z, ext->invDiag, ext->w, &a.st->done, s));
+      } else {
+        k_update<T><<<vec_grid(Nall), RT, 0, s>>>(a);
+        NEKB_CUDA(cudaGetLastError());
+        NEKB_TRY(net_precondition(ext->bp, ext->net, a.r, a.z, ext->invDiag, ext->w, &a.st->done, s));
+      }
     } else {
       return fail(NEKB_ERR_UNSUPPORTED, "learned preconditioner runs in FP32 only");
     }
@@ -921,8 +931,7 @@ int ensure_jacobi64(nekb_bp* bp, int bk, const double* lambda)
     k_mask_set<<<vec_grid(bp->Nmasked), RT, 0, s>>>(bp->Nmasked, bp->mask.as<int32_t>(), 1.0, d);
     NEKB_CUDA(cudaGetLastError());
   }
-  NEKB_TRY(launch_gs_add(bp->ogs->Nmulti, bp->ogs->d_offsets, bp->ogs->d_ids, 1, bp->offset, d,
-                         NEKB_DOUBLE, nullptr, s));
+  NEKB_TRY(launch_gs_add(bp->ogs, 1, bp->offset, d, NEKB_DOUBLE, nullptr, s));
   NEKB_TRY(launch_vec_inv(d, bp->offset, s));
   return NEKB_OK;
 }
