@@ -319,6 +319,7 @@ nekb_bp* nekb_bp_create_mesh(int N, int64_t E, int Nfields, const double* ggeo, 
 void nekb_ogs_release(nekb_ogs* o)
 {
   if (!o) return;
+  cudaFree(o->d_chunks);
   cudaFree(o->d_pairs);
   cudaFree(o->d_quads);
   cudaFree(o->d_offsets);

@@ -209,12 +209,20 @@ int nekb_ogs_build(nekb_ogs* o, int64_t N, const int64_t* ids)
     const double v = 1.0 / (double)(e - s);
     for (int32_t n = s; n < e; ++n) invdeg[o->h_ids[n]] = v;
   }
-  // the groups with more than one member, for the device kernel: groups of
-  // two and of four as packed member ids, the others as a compact CSR
-  std::vector<int32_t> pairs, quads, moff(1, 0), mids;
+  // the groups with more than one member, for the device kernel: in CSR
+  // order, chunks of kGsChunk groups (a chunk's nodes lie close together, so
+  // one CTA's loads share sectors), each split into groups of two and of four
+  // (packed member ids) and the others (a compact CSR)
+  std::vector<int32_t> pairs, quads, moff(1, 0), mids, chunks;
+  int64_t nm = 0;
   for (int64_t q = 0; q < Ng; ++q) {
     const int32_t s = o->h_offsets[q], e = o->h_offsets[q + 1];
     if (e - s < 2) continue;
+    if (nm++ % nekb_ogs::kGsChunk == 0) {
+      chunks.push_back((int32_t)(pairs.size() / 2));
+      chunks.push_back((int32_t)(quads.size() / 4));
+      chunks.push_back((int32_t)(moff.size() - 1));
+    }
     std::vector<int32_t>& dst = e - s == 2 ? pairs : (e - s == 4 ? quads : mids);
     for (int32_t n = s; n < e; ++n) dst.push_back(o->h_ids[n]);
     if (e - s != 2 && e - s != 4) moff.push_back((int32_t)mids.size());
@@ -223,12 +231,17 @@ int nekb_ogs_build(nekb_ogs* o, int64_t N, const int64_t* ids)
   o->Nquads = (int64_t)quads.size() / 4;
   o->Nrest = (int64_t)moff.size() - 1;
   o->Nmulti = o->Npairs + o->Nquads + o->Nrest;
+  o->Nchunks = (int64_t)chunks.size() / 3;
+  chunks.push_back((int32_t)o->Npairs);
+  chunks.push_back((int32_t)o->Nquads);
+  chunks.push_back((int32_t)o->Nrest);
   auto upload = [](int32_t** d, const std::vector<int32_t>& h) -> int {
     if (h.empty()) return NEKB_OK;
     NEKB_CUDA(cudaMalloc(d, sizeof(int32_t) * h.size()));
     NEKB_CUDA(cudaMemcpy(*d, h.data(), sizeof(int32_t) * h.size(), cudaMemcpyHostToDevice));
     return NEKB_OK;
   };
+  NEKB_TRY(upload(&o->d_chunks, chunks));
   NEKB_TRY(upload(&o->d_pairs, pairs));
   NEKB_TRY(upload(&o->d_quads, quads));
   NEKB_TRY(upload(&o->d_offsets, moff));

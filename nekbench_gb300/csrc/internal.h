@@ -131,10 +131,13 @@ struct nekb_ogs {
   int64_t Nmulti = 0;                 // groups with more than one member
   std::vector<int32_t> h_offsets;     // NlocalGather+1 (reference CSR, host)
   std::vector<int32_t> h_ids;         // Nlocal
-  // device copy of the multi-member groups by size: groups of two and of four
+  // device copy of the multi-member groups, cut in CSR order into chunks of
+  // kGsChunk groups and, within a chunk, by size: groups of two and of four
   // as packed member ids (a box mesh's face and edge nodes), every other size
   // as CSR; members in CSR order within each group
-  int64_t Npairs = 0, Nquads = 0, Nrest = 0;
+  static constexpr int kGsChunk = 2048;
+  int64_t Npairs = 0, Nquads = 0, Nrest = 0, Nchunks = 0;
+  int32_t* d_chunks = nullptr;        // 3 (Nchunks+1): first pair, quad, other group of each chunk
   int32_t* d_pairs = nullptr;         // 2 Npairs
   int32_t* d_quads = nullptr;         // 4 Nquads
   int32_t* d_offsets = nullptr;       // Nrest+1

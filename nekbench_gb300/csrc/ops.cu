@@ -235,16 +235,20 @@ __global__ void k_trilinear_coeffs(int64_t E, const double* __restrict__ EX,
 // results are deterministic and equal to the CPU's.
 //
 // The kernel is bound by the latency of its dependent loads (group -> member
-// ids -> values), not by bandwidth.  Groups of two and of four members (on a
-// box mesh: the nodes inside element faces and along element edges, 97 % of
-// the shared nodes) come as packed member ids, one 8- or 16-byte load per
-// group; the other groups keep the CSR (offsets -> ids -> values).  Each
+// ids -> values) and by the scattered 4-byte accesses, not by bandwidth.
+// Groups of two and of four members (on a box mesh: the nodes inside element
+// faces and along element edges, 97 % of the shared nodes) come as packed
+// member ids, one 8- or 16-byte load per group; the other groups keep the CSR
+// (offsets -> ids -> values).  The groups are cut, in CSR order, into chunks
+// of nekb_ogs::kGsChunk groups, one CTA per chunk, so the face, edge and corner
+// nodes of the same elements are summed together and share sectors.  Each
 // thread takes kGsGroups groups at a time and issues the loads of all of them
 // before it sums.
-constexpr int kGsGroups = 4;
+constexpr int kGsGroups = 4, kGsThreads = 256;
 
 struct GsGroups {
-  int64_t Npairs, Nquads, Nrest;
+  int64_t Nchunks;
+  const int32_t* chunks;  // first pair, quad and other group of chunk c at 3 c
   const int2* pairs;
   const int4* quads;
   const int32_t* offsets;
@@ -252,94 +256,98 @@ struct GsGroups {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_gs_add(GsGroups g, int k, int64_t stride, T* __restrict__ q,
-                                                const int* skip)
+__global__ void __launch_bounds__(kGsThreads) k_gs_add(GsGroups g, int k, int64_t stride, T* __restrict__ q,
+                                                       const int* skip)
 {
   if (skip != nullptr && *skip != 0) return;
-  const int64_t step = (int64_t)gridDim.x * blockDim.x;
-  const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  for (int f = 0; f < k; ++f) {
-    T* qf = q + f * stride;
-    for (int64_t p0 = t0; p0 < g.Npairs; p0 += kGsGroups * step) {
-      int2 m[kGsGroups];
+  const int tid = threadIdx.x;
+  constexpr int kStep = kGsThreads;
+  for (int64_t c = blockIdx.x; c < g.Nchunks; c += gridDim.x) {
+    const int32_t* ch = g.chunks + 3 * c;
+    const int32_t p_lo = ch[0], p_hi = ch[3], q_lo = ch[1], q_hi = ch[4], o_lo = ch[2], o_hi = ch[5];
+    for (int f = 0; f < k; ++f) {
+      T* qf = q + f * stride;
+      for (int32_t p0 = p_lo + tid; p0 < p_hi; p0 += kGsGroups * kStep) {
+        int2 m[kGsGroups];
 #pragma unroll
-      for (int u = 0; u < kGsGroups; ++u) {
-        const int64_t p = p0 + u * step;
-        m[u] = p < g.Npairs ? g.pairs[p] : make_int2(-1, -1);
-      }
-      T a[kGsGroups], b[kGsGroups];
+        for (int u = 0; u < kGsGroups; ++u) {
+          const int32_t p = p0 + u * kStep;
+          m[u] = p < p_hi ? g.pairs[p] : make_int2(-1, -1);
+        }
+        T a[kGsGroups], b[kGsGroups];
 #pragma unroll
-      for (int u = 0; u < kGsGroups; ++u) {
-        a[u] = m[u].x >= 0 ? qf[m[u].x] : T(0);
-        b[u] = m[u].x >= 0 ? qf[m[u].y] : T(0);
-      }
+        for (int u = 0; u < kGsGroups; ++u) {
+          a[u] = m[u].x >= 0 ? qf[m[u].x] : T(0);
+          b[u] = m[u].x >= 0 ? qf[m[u].y] : T(0);
+        }
 #pragma unroll
-      for (int u = 0; u < kGsGroups; ++u) {
-        if (m[u].x >= 0) {
-          const T sum = a[u] + b[u];  // (0 + a) + b: the CSR-order sum
-          qf[m[u].x] = sum;
-          qf[m[u].y] = sum;
+        for (int u = 0; u < kGsGroups; ++u) {
+          if (m[u].x >= 0) {
+            const T sum = a[u] + b[u];  // (0 + a) + b: the CSR-order sum
+            qf[m[u].x] = sum;
+            qf[m[u].y] = sum;
+          }
         }
       }
-    }
-    for (int64_t p0 = t0; p0 < g.Nquads; p0 += kGsGroups * step) {
-      int4 m[kGsGroups];
+      for (int32_t p0 = q_lo + tid; p0 < q_hi; p0 += kGsGroups * kStep) {
+        int4 m[kGsGroups];
 #pragma unroll
-      for (int u = 0; u < kGsGroups; ++u) {
-        const int64_t p = p0 + u * step;
-        m[u] = p < g.Nquads ? g.quads[p] : make_int4(-1, -1, -1, -1);
-      }
-      T v[kGsGroups][4];
+        for (int u = 0; u < kGsGroups; ++u) {
+          const int32_t p = p0 + u * kStep;
+          m[u] = p < q_hi ? g.quads[p] : make_int4(-1, -1, -1, -1);
+        }
+        T v[kGsGroups][4];
 #pragma unroll
-      for (int u = 0; u < kGsGroups; ++u) {
-        const bool on = m[u].x >= 0;
-        v[u][0] = on ? qf[m[u].x] : T(0);
-        v[u][1] = on ? qf[m[u].y] : T(0);
-        v[u][2] = on ? qf[m[u].z] : T(0);
-        v[u][3] = on ? qf[m[u].w] : T(0);
-      }
+        for (int u = 0; u < kGsGroups; ++u) {
+          const bool on = m[u].x >= 0;
+          v[u][0] = on ? qf[m[u].x] : T(0);
+          v[u][1] = on ? qf[m[u].y] : T(0);
+          v[u][2] = on ? qf[m[u].z] : T(0);
+          v[u][3] = on ? qf[m[u].w] : T(0);
+        }
 #pragma unroll
-      for (int u = 0; u < kGsGroups; ++u) {
-        if (m[u].x >= 0) {
-          const T sum = ((v[u][0] + v[u][1]) + v[u][2]) + v[u][3];
-          qf[m[u].x] = sum;
-          qf[m[u].y] = sum;
-          qf[m[u].z] = sum;
-          qf[m[u].w] = sum;
+        for (int u = 0; u < kGsGroups; ++u) {
+          if (m[u].x >= 0) {
+            const T sum = ((v[u][0] + v[u][1]) + v[u][2]) + v[u][3];
+            qf[m[u].x] = sum;
+            qf[m[u].y] = sum;
+            qf[m[u].z] = sum;
+            qf[m[u].w] = sum;
+          }
         }
       }
-    }
-    for (int64_t g0 = t0; g0 < g.Nrest; g0 += kGsGroups * step) {
-      int32_t st[kGsGroups], en[kGsGroups], i0[kGsGroups], i1[kGsGroups];
+      for (int32_t g0 = o_lo + tid; g0 < o_hi; g0 += kGsGroups * kStep) {
+        int32_t st[kGsGroups], en[kGsGroups], i0[kGsGroups], i1[kGsGroups];
 #pragma unroll
-      for (int u = 0; u < kGsGroups; ++u) {
-        const int64_t gid = g0 + u * step;
-        st[u] = en[u] = 0;
-        if (gid < g.Nrest) {
-          st[u] = g.offsets[gid];
-          en[u] = g.offsets[gid + 1];
+        for (int u = 0; u < kGsGroups; ++u) {
+          const int32_t gid = g0 + u * kStep;
+          st[u] = en[u] = 0;
+          if (gid < o_hi) {
+            st[u] = g.offsets[gid];
+            en[u] = g.offsets[gid + 1];
+          }
         }
-      }
 #pragma unroll
-      for (int u = 0; u < kGsGroups; ++u) {
-        i0[u] = st[u] < en[u] ? g.ids[st[u]] : -1;
-        i1[u] = st[u] + 1 < en[u] ? g.ids[st[u] + 1] : -1;
-      }
-      T sm[kGsGroups];
+        for (int u = 0; u < kGsGroups; ++u) {
+          i0[u] = st[u] < en[u] ? g.ids[st[u]] : -1;
+          i1[u] = st[u] + 1 < en[u] ? g.ids[st[u] + 1] : -1;
+        }
+        T sm[kGsGroups];
 #pragma unroll
-      for (int u = 0; u < kGsGroups; ++u) {
-        const T a = i0[u] >= 0 ? qf[i0[u]] : T(0);
-        const T b = i1[u] >= 0 ? qf[i1[u]] : T(0);
-        sm[u] = a + b;  // (0 + a) + b: the CSR-order sum of the first two members
-      }
+        for (int u = 0; u < kGsGroups; ++u) {
+          const T a = i0[u] >= 0 ? qf[i0[u]] : T(0);
+          const T b = i1[u] >= 0 ? qf[i1[u]] : T(0);
+          sm[u] = a + b;  // (0 + a) + b: the CSR-order sum of the first two members
+        }
 #pragma unroll
-      for (int u = 0; u < kGsGroups; ++u)
-        for (int32_t n = st[u] + 2; n < en[u]; ++n) sm[u] += qf[g.ids[n]];
+        for (int u = 0; u < kGsGroups; ++u)
+          for (int32_t n = st[u] + 2; n < en[u]; ++n) sm[u] += qf[g.ids[n]];
 #pragma unroll
-      for (int u = 0; u < kGsGroups; ++u) {
-        if (i0[u] >= 0) qf[i0[u]] = sm[u];
-        if (i1[u] >= 0) qf[i1[u]] = sm[u];
-        for (int32_t n = st[u] + 2; n < en[u]; ++n) qf[g.ids[n]] = sm[u];
+        for (int u = 0; u < kGsGroups; ++u) {
+          if (i0[u] >= 0) qf[i0[u]] = sm[u];
+          if (i1[u] >= 0) qf[i1[u]] = sm[u];
+          for (int32_t n = st[u] + 2; n < en[u]; ++n) qf[g.ids[n]] = sm[u];
+        }
       }
     }
   }
@@ -469,14 +477,13 @@ int launch_gs_add(const nekb_ogs* ogs, int k, int64_t stride, void* q, int dtype
                   cudaStream_t s)
 {
   if (ogs->Nmulti == 0) return NEKB_OK;
-  const GsGroups g{ogs->Npairs, ogs->Nquads, ogs->Nrest, reinterpret_cast<const int2*>(ogs->d_pairs),
+  const GsGroups g{ogs->Nchunks, ogs->d_chunks, reinterpret_cast<const int2*>(ogs->d_pairs),
                    reinterpret_cast<const int4*>(ogs->d_quads), ogs->d_offsets, ogs->d_ids};
-  const int64_t most = std::max(ogs->Npairs, std::max(ogs->Nquads, ogs->Nrest));
-  const unsigned grid = grid_for((most + kGsGroups - 1) / kGsGroups, 256, 152 * 32);
+  const unsigned grid = (unsigned)std::min<int64_t>(ogs->Nchunks, 152 * 64);
   if (dtype == NEKB_DOUBLE)
-    k_gs_add<double><<<grid, 256, 0, s>>>(g, k, stride, (double*)q, skip);
+    k_gs_add<double><<<grid, kGsThreads, 0, s>>>(g, k, stride, (double*)q, skip);
   else if (dtype == NEKB_FLOAT)
-    k_gs_add<float><<<grid, 256, 0, s>>>(g, k, stride, (float*)q, skip);
+    k_gs_add<float><<<grid, kGsThreads, 0, s>>>(g, k, stride, (float*)q, skip);
   else
     return fail(NEKB_ERR_UNSUPPORTED, "gather-scatter: dtype %d", dtype);
   NEKB_CUDA(cudaGetLastError());
