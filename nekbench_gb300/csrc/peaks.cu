@@ -1,4 +1,4 @@
-// Microbenchmarks of the device roofs the kernels are judged against:
+// Microbenchmarks of the device roofs the kernels are measured against:
 // FMA throughput (FP64 or FP32, CUDA cores) and device-to-device copy bandwidth.
 #include "internal.h"
 
