@@ -224,11 +224,12 @@ __device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity)
   return false;
 }
 
+// sum over the CTA; the previous call's reads of red are separated from this
+// call's writes by the barriers of the element in between
 __device__ __forceinline__ float block_sum4(float v, float* red)
 {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  __syncthreads();
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
   return red[0] + red[1] + red[2] + red[3];
