@@ -286,13 +286,17 @@ def test_config1_e512_against_axhelm_reference(nb, O, dev):
         assert rel(got, ref) < 1e-12
 
 
+@pytest.mark.parametrize("prec", ["FP64", "FP64_SPLIT"])
 @pytest.mark.parametrize("N", [5, 7, 8])
 @pytest.mark.parametrize("flags", [0, 1, 2, 7])
-def test_fp64_any_derivative_matrix(nb, O, dev, N, flags):
-    """The FP64 kernel evaluates the even-odd form only for a centro-
-    antisymmetric D (nodes symmetric about the element centre); for any other
-    D it must evaluate the direct sums.  A random D, and a GLL D with one entry
-    moved by 1e-9, against the oracle at 1e-12."""
+def test_fp64_any_derivative_matrix(nb, O, dev, N, flags, prec):
+    """The FP64 and double-float kernels evaluate the even-odd form only for a
+    centro-antisymmetric D (nodes symmetric about the element centre); for any
+    other D they must evaluate the direct sums.  A random D, and a GLL D with
+    one entry moved by 1e-9, against the oracle at 1e-12 (the double-float
+    precision has no Partial forms)."""
+    if prec == "FP64_SPLIT" and flags & nb.AX_PARTIAL:
+        pytest.skip("Partial variants run in FP64")
     m = O.BoxMesh(N, 3, 2, 2, perturb=0.1, seed=60 + N)
     E, L = m.E, m.Nlocal
     nf = 3 if flags & nb.AX_N3 else 1
@@ -311,7 +315,7 @@ def test_fp64_any_derivative_matrix(nb, O, dev, N, flags):
         else:
             ref = O.axhelm(N + 1, E, L, flags, m.ggeo, D, lam, q)
             Aq = torch.zeros(nf * L, dtype=torch.float64, device=dev)
-            nb.axhelm(N + 1, flags, nb.FP64, E, L, T(m.ggeo, dev), T(D, dev), T(lam, dev),
+            nb.axhelm(N + 1, flags, getattr(nb, prec), E, L, T(m.ggeo, dev), T(D, dev), T(lam, dev),
                       T(q, dev), Aq)
         torch.cuda.synchronize()
         assert rel(Aq.cpu().numpy(), ref) < 1e-12
