@@ -319,3 +319,34 @@ def test_fp64_any_derivative_matrix(nb, O, dev, N, flags, prec):
                       T(q, dev), Aq)
         torch.cuda.synchronize()
         assert rel(Aq.cpu().numpy(), ref) < 1e-12
+
+
+def test_overlap_form_of_the_operator(nb, dev):
+    """BPAxOperator's overlap form (nekBone/solve.cpp:189-211): the operator on
+    the elements whose nodes other ranks share, the gather-scatter started, the
+    operator on the other elements, the gather-scatter finished.  On one GPU it
+    is composed from the Partial operator over the two element lists and one
+    gather-scatter after both; for any partition of the elements the result is
+    the plain operator followed by the gather-scatter, bit for bit."""
+    N = 7
+    bp = nb.BP(N, 4, 3, 3, perturb=0.1, seed=11)
+    E, L = bp.E, bp.Nlocal
+    ggeo = bp.device_array("ggeo", 7 * L, torch.float64)
+    D = bp.device_array("D", (N + 1) ** 2, torch.float64)
+    g = torch.Generator(device="cpu").manual_seed(5)
+    q = torch.rand(L, generator=g, dtype=torch.float64).to(dev)
+    lam = (torch.rand(2 * L, generator=g, dtype=torch.float64) + 0.5).to(dev)
+    every = np.arange(E, dtype=np.int32)
+    halo = torch.from_numpy(every[every % 3 == 0].copy()).to(dev)
+    interior = torch.from_numpy(every[every % 3 != 0].copy()).to(dev)
+    for flags in (0, nb.AX_BK):
+        full = torch.zeros(L, dtype=torch.float64, device=dev)
+        nb.axhelm(N + 1, flags, nb.FP64, E, L, ggeo, D, lam, q, full)
+        bp.ogs.gather_scatter_many(full)
+        split = torch.zeros(L, dtype=torch.float64, device=dev)
+        for part in (halo, interior):
+            nb.axhelm(N + 1, flags | nb.AX_PARTIAL, nb.FP64, len(part), L, ggeo, D, lam, q, split,
+                      element_list=part)
+        bp.ogs.gather_scatter_many(split)
+        torch.cuda.synchronize()
+        assert torch.equal(split, full), flags
