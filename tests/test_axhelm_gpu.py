@@ -133,7 +133,7 @@ def test_reference_driver_inputs(nb, O, dev):
         assert rel(Aq.cpu().numpy(), ref) < 1e-12
 
 
-@pytest.mark.parametrize("N", [3, 7, 9])
+@pytest.mark.parametrize("N", [3, 7, 8, 9, 10, 11])
 @pytest.mark.parametrize("flags", [0, 1, 2])
 def test_fp32(nb, O, dev, N, flags):
     m = O.BoxMesh(N, 3, 3, 2, perturb=0.1, seed=21)
