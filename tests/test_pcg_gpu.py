@@ -132,6 +132,29 @@ def test_mixed_three_fields(nb, O, dev):
     assert true_rel_res(obp, f, x_d.cpu().numpy()) <= 1.01e-10
 
 
+def test_learned_three_fields(nb, O, dev):
+    """The learned preconditioner on a three-field problem: the network runs
+    over the 3 E element copies and, on the tcgen05 kernel, folds the flexible
+    CG's update into them; the solve reaches the true FP64 residual (checked
+    by the oracle) in about the iterations of the mma.sync kernel, whose update
+    is a separate pass."""
+    import os
+    bp, m = pair(nb, O, 7, 3, Nfields=3)
+    obp, lam, f = problem(O, m, 3, 18)
+    net = nb.Net.load(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                   "nekbench_gb300", "weights", "precond_n7_c16.bin"))
+    its = {}
+    for mode in (nb.NET_TENSOR_TC5, nb.NET_TENSOR_SYNC):
+        net.inference = mode
+        r_d, x_d = T(f, dev), torch.zeros(len(f), dtype=torch.float64, device=dev)
+        st = bp.pcg(T(lam, dev), r_d, x_d, 1e-8, 3000, solver=nb.SOLVER_MIXED,
+                    precond=nb.PRECOND_LEARNED, net=net)
+        assert st["status"] == 0 and st["true_rel_res"] <= 1e-8, (mode, st)
+        assert true_rel_res(obp, f, x_d.cpu().numpy()) <= 1.01e-8, mode
+        its[mode] = st["iterations"]
+    assert abs(its[nb.NET_TENSOR_TC5] - its[nb.NET_TENSOR_SYNC]) <= 0.1 * its[nb.NET_TENSOR_SYNC] + 5, its
+
+
 def test_mixed_keeps_krylov_information(nb, O, dev):
     """Residual replacement keeps the FP32 iteration count close to the FP64 one
     (restarted refinement would repeat the early iterations)."""
